@@ -1,0 +1,142 @@
+"""ctypes binding of the in-tree libcufinufft.so (the GB300 NUFFT engine).
+
+The struct layouts mirror include/cufinufft_opts.h and include/gbnufft_ext.h.
+Loading fails loudly when the shared library has not been built: there is no
+fallback implementation.
+"""
+import ctypes
+import os
+from ctypes import (POINTER, Structure, c_double, c_float, c_int, c_int64, c_size_t,
+                    c_void_p)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libcufinufft.so")
+
+
+class CufinufftOpts(Structure):
+    """Same field order and types as cufinufft_opts (include/cufinufft_opts.h)."""
+
+    _fields_ = [
+        ("upsampfac", c_double),
+        ("gpu_method", c_int),
+        ("gpu_sort", c_int),
+        ("gpu_binsizex", c_int),
+        ("gpu_binsizey", c_int),
+        ("gpu_binsizez", c_int),
+        ("gpu_obinsizex", c_int),
+        ("gpu_obinsizey", c_int),
+        ("gpu_obinsizez", c_int),
+        ("gpu_maxsubprobsize", c_int),
+        ("gpu_kerevalmeth", c_int),
+        ("gpu_spreadinterponly", c_int),
+        ("gpu_maxbatchsize", c_int),
+        ("gpu_device_id", c_int),
+        ("gpu_stream", c_void_p),
+        ("modeord", c_int),
+        ("gpu_np", c_int),
+        ("debug", c_int),
+    ]
+
+
+class PlanInfo(Structure):
+    """gbnufft_plan_info (include/gbnufft_ext.h)."""
+
+    _fields_ = [
+        ("type", c_int), ("dim", c_int), ("ntransf", c_int), ("batchsize", c_int),
+        ("ns", c_int), ("beta", c_double), ("upsampfac", c_double),
+        ("nf", c_int * 3), ("bins", c_int * 3), ("method", c_int), ("nsub", c_int),
+        ("M", c_int64), ("N", c_int64), ("spread_smem", c_size_t),
+        ("horner_err", c_double), ("inner_nf", c_int * 3),
+    ]
+
+
+class FinufftOpts(Structure):
+    """Same layout as finufft_opts (include/finufft.h)."""
+
+    _fields_ = [
+        ("modeord", c_int), ("spreadinterponly", c_int), ("debug", c_int),
+        ("spread_debug", c_int), ("showwarn", c_int), ("nthreads", c_int), ("fftw", c_int),
+        ("spread_sort", c_int), ("spread_kerevalmeth", c_int), ("spread_kerpad", c_int),
+        ("upsampfac", c_double), ("spread_thread", c_int), ("maxbatchsize", c_int),
+        ("spread_nthr_atomic", c_int), ("spread_max_sp_size", c_int),
+        ("spread_kerformula", c_int), ("allow_eps_too_small", c_int),
+        ("fftw_lock_fun", c_void_p), ("fftw_unlock_fun", c_void_p),
+        ("fftw_lock_data", c_void_p),
+    ]
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the engine library (raises OSError when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(
+            "GB300 NUFFT library not built (%s missing): run "
+            "`python -c 'import __graft_entry__ as g; g.build()'` first" % path)
+    lib = ctypes.CDLL(path)
+    _declare(lib)
+    _lib = lib
+    return lib
+
+
+def _declare(lib):
+    i64p = POINTER(c_int64)
+    for pfx, real in (("cufinufft", c_double), ("cufinufftf", c_float)):
+        f = getattr(lib, pfx + "_makeplan")
+        f.argtypes = [c_int, c_int, i64p, c_int, c_int, real, POINTER(c_void_p),
+                      POINTER(CufinufftOpts)]
+        f.restype = c_int
+        f = getattr(lib, pfx + "_setpts")
+        f.argtypes = [c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
+                      c_void_p, c_void_p]
+        f.restype = c_int
+        for name in ("_execute", "_execute_adjoint", "_graph_capture"):
+            f = getattr(lib, pfx + name)
+            f.argtypes = [c_void_p, c_void_p, c_void_p]
+            f.restype = c_int
+        for name in ("_destroy", "_graph_launch"):
+            f = getattr(lib, pfx + name)
+            f.argtypes = [c_void_p]
+            f.restype = c_int
+        f = getattr(lib, pfx + "_plan_info")
+        f.argtypes = [c_void_p, POINTER(PlanInfo)]
+        f.restype = c_int
+        f = getattr(lib, pfx + "_stage_times")
+        f.argtypes = [c_void_p, c_int, POINTER(c_float)]
+        f.restype = c_int
+        f = getattr(lib, pfx + "_get_sort")
+        f.argtypes = [c_void_p, c_void_p, c_void_p]
+        f.restype = c_int
+    lib.cufinufft_default_opts.argtypes = [POINTER(CufinufftOpts)]
+    lib.cufinufft_default_opts.restype = None
+    lib.finufft_default_opts.argtypes = [POINTER(FinufftOpts)]
+    lib.finufft_default_opts.restype = None
+    lib.gbnufft_version.restype = ctypes.c_char_p
+    lib.gbnufft_smem_atomic_rate.argtypes = [c_int, POINTER(c_double)]
+    lib.gbnufft_smem_atomic_rate.restype = c_int
+    for pfx, real in (("finufft", c_double), ("finufftf", c_float)):
+        f = getattr(lib, pfx + "_makeplan")
+        f.argtypes = [c_int, c_int, i64p, c_int, c_int, real, POINTER(c_void_p),
+                      POINTER(FinufftOpts)]
+        f.restype = c_int
+        f = getattr(lib, pfx + "_setpts")
+        f.argtypes = [c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
+                      c_void_p, c_void_p]
+        f.restype = c_int
+        for name in ("_execute", "_execute_adjoint"):
+            f = getattr(lib, pfx + name)
+            f.argtypes = [c_void_p, c_void_p, c_void_p]
+            f.restype = c_int
+        f = getattr(lib, pfx + "_destroy")
+        f.argtypes = [c_void_p]
+        f.restype = c_int
+
+
+def default_opts():
+    o = CufinufftOpts()
+    load().cufinufft_default_opts(ctypes.byref(o))
+    return o

@@ -1,0 +1,80 @@
+// Shared definitions for the GB300 NUFFT engine: complex types, error
+// propagation and the plain-old-data structs that kernels receive by value.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <type_traits>
+
+#include "finufft_errors.h"
+
+namespace gbn {
+
+constexpr int MAX_NS = 16;       // widest kernel (double precision)
+constexpr int MAX_NS_FLOAT = 12; // widest kernel in single precision
+constexpr int MAX_HCOEF = 24;    // max coefficients of one Horner piece
+constexpr int MAX_NQUAD = 100;   // max Gauss-Legendre nodes for kernel transforms
+constexpr double PI = 3.141592653589793238462643383279502884;
+constexpr double INV_2PI = 0.159154943091895335768883763372514362;
+
+template <typename T> struct cplx_t;
+template <> struct cplx_t<float> { using type = float2; };
+template <> struct cplx_t<double> { using type = double2; };
+template <typename T> using cplx = typename cplx_t<T>::type;
+
+// Number of Horner coefficients used for kernel width ns: pieces are fitted
+// with at most this many and zero-padded at the high-degree end, so the
+// evaluation loop has a compile-time trip count.
+__host__ __device__ constexpr int horner_len(int ns) {
+  return ns + 6 < MAX_HCOEF ? ns + 6 : MAX_HCOEF;
+}
+
+// Exception carrying a FINUFFT error code; caught at the C-ABI boundary.
+struct Error {
+  int code;
+  const char *msg;
+};
+
+#define GBN_THROW(code_, msg_) throw ::gbn::Error{(code_), (msg_)}
+#define GBN_CUDA(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      fprintf(stderr, "[gbnufft] CUDA error %s at %s:%d\n", cudaGetErrorString(e_),      \
+              __FILE__, __LINE__);                                                       \
+      throw ::gbn::Error{FINUFFT_ERR_CUDA_FAILURE, cudaGetErrorString(e_)};              \
+    }                                                                                    \
+  } while (0)
+#define GBN_LAUNCH_CHECK() GBN_CUDA(cudaGetLastError())
+
+// ES ("exponential of semicircle") kernel phi(x) = exp(beta*(sqrt(1-(2x/ns)^2)-1)),
+// |x| < ns/2, and its piecewise-polynomial (Horner) form: piece j covers
+// x in [-ns/2+j, -ns/2+j+1], written as a polynomial in u = 2*(x - piece start) - 1.
+// coef[k][j] is the coefficient of u^(ndeg-1-k) of piece j (highest degree first).
+template <typename T> struct KernelShape {
+  int ns;
+  int use_horner; // 1: Horner pieces, 0: direct exp(sqrt())
+  int ncoef;      // number of Horner coefficients per piece
+  int pad_;
+  T beta;
+  T es_c; // (2/ns)^2
+  T coef[MAX_HCOEF][MAX_NS];
+};
+
+// Where the nonuniform points sit after the device bin sort, and how the
+// fine grid is tiled. Passed by value to spread/interp kernels.
+template <typename T> struct PointLayout {
+  int dim;
+  int nf[3];       // fine grid size per dimension
+  int bin[3];      // bin (tile interior) size per dimension
+  int nbin[3];     // number of bins per dimension
+  int M;           // number of points
+  int nsub;        // number of subproblems
+  const int *sub_bin;   // subproblem -> bin index (x fastest)
+  const int *sub_start; // subproblem -> first sorted point
+  const int *sub_count; // subproblem -> number of points
+  const int *perm;      // sorted position -> user index
+  const T *loc[3];      // sorted bin-local coordinates in grid units, [0, bin]
+};
+
+} // namespace gbn

@@ -1,0 +1,376 @@
+// Deconvolution / amplification, kernel Fourier series and type-3 phase
+// kernels, plus the host dispatch of the spread/interp translation units.
+#include <vector>
+
+#include "device_util.cuh"
+#include "elementwise.h"
+#include "spreadinterp.h"
+
+namespace gbn {
+
+template <typename T, int DIM>
+void spread_dim(const PointLayout<T> &, const KernelShape<T> &, const cplx<T> *,
+                const cplx<T> *, int, cplx<T> *, int64_t, int, const SpreadConfig &,
+                cudaStream_t);
+template <typename T, int DIM>
+void interp_dim(const PointLayout<T> &, const KernelShape<T> &, const cplx<T> *, int64_t,
+                const cplx<T> *, int, cplx<T> *, int, cudaStream_t);
+
+template <typename T> size_t spread_tile_smem(int dim, int ns, const int bin[3]) {
+  auto pitch = [&](int tx) {
+    return dim == 3 ? (tx <= 8 ? 8 : 16 * ((tx - 8 + 15) / 16) + 8) : tx;
+  };
+  size_t cells = (size_t)pitch(bin[0] + ns);
+  if (dim > 1) cells *= (size_t)(bin[1] + ns);
+  if (dim > 2) cells *= (size_t)(bin[2] + ns);
+  return 2 * sizeof(T) * cells;
+}
+template size_t spread_tile_smem<float>(int, int, const int[3]);
+template size_t spread_tile_smem<double>(int, int, const int[3]);
+
+template <typename T>
+void launch_spread(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *c,
+                   const cplx<T> *pre, int conj_pre, cplx<T> *fw, int64_t nf_total, int ntr,
+                   const SpreadConfig &cfg, cudaStream_t s) {
+  if (L.nsub <= 0 || ntr <= 0) return;
+  if (L.dim == 1) spread_dim<T, 1>(L, K, c, pre, conj_pre, fw, nf_total, ntr, cfg, s);
+  else if (L.dim == 2) spread_dim<T, 2>(L, K, c, pre, conj_pre, fw, nf_total, ntr, cfg, s);
+  else spread_dim<T, 3>(L, K, c, pre, conj_pre, fw, nf_total, ntr, cfg, s);
+}
+template <typename T>
+void launch_interp(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *fw,
+                   int64_t nf_total, const cplx<T> *post, int conj_post, cplx<T> *out, int ntr,
+                   cudaStream_t s) {
+  if (L.nsub <= 0 || ntr <= 0) return;
+  if (L.dim == 1) interp_dim<T, 1>(L, K, fw, nf_total, post, conj_post, out, ntr, s);
+  else if (L.dim == 2) interp_dim<T, 2>(L, K, fw, nf_total, post, conj_post, out, ntr, s);
+  else interp_dim<T, 3>(L, K, fw, nf_total, post, conj_post, out, ntr, s);
+}
+template void launch_spread<float>(const PointLayout<float> &, const KernelShape<float> &,
+                                   const float2 *, const float2 *, int, float2 *, int64_t, int,
+                                   const SpreadConfig &, cudaStream_t);
+template void launch_spread<double>(const PointLayout<double> &, const KernelShape<double> &,
+                                    const double2 *, const double2 *, int, double2 *, int64_t,
+                                    int, const SpreadConfig &, cudaStream_t);
+template void launch_interp<float>(const PointLayout<float> &, const KernelShape<float> &,
+                                   const float2 *, int64_t, const float2 *, int, float2 *, int,
+                                   cudaStream_t);
+template void launch_interp<double>(const PointLayout<double> &, const KernelShape<double> &,
+                                    const double2 *, int64_t, const double2 *, int, double2 *,
+                                    int, cudaStream_t);
+
+namespace {
+inline unsigned blocks_for(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b > 152 * 32) b = 152 * 32;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+// mode index of fk position i along one axis of length m
+__device__ __forceinline__ int mode_of(int i, int m, int modeord) {
+  return modeord == 0 ? i - m / 2 : (i < m - m / 2 ? i : i - m);
+}
+// fk position of mode k along one axis of length m
+__device__ __forceinline__ int pos_of(int k, int m, int modeord) {
+  return modeord == 0 ? k + m / 2 : (k >= 0 ? k : k + m);
+}
+
+template <typename T>
+__global__ void inv_fseries_kernel(int nf, QuadNodes Q, T *inv) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= nf / 2; k += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int n = 0; n < Q.q; ++n) acc += Q.f[n] * 2.0 * cos((double)k * (2.0 * PI * Q.z[n] / nf));
+    if (k & 1) acc = -acc; // grid origin sits at x = -pi
+    inv[k] = (T)(1.0 / acc);
+  }
+}
+
+template <typename T, int DIM>
+__global__ void deconv_kernel(int ms0, int ms1, int ms2, int nf0, int nf1, int nf2, int modeord,
+                              const T *__restrict__ i0, const T *__restrict__ i1,
+                              const T *__restrict__ i2, const cplx<T> *__restrict__ fw,
+                              int64_t nf_total, cplx<T> *__restrict__ fk, int64_t nmodes, int ntr) {
+  const int64_t total = nmodes * ntr;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int tr = (int)(q / nmodes);
+    const int64_t i = q - (int64_t)tr * nmodes;
+    const int ix = (int)(i % ms0);
+    const int kx = mode_of(ix, ms0, modeord);
+    int64_t g = kx >= 0 ? kx : nf0 + kx;
+    T f = i0[kx >= 0 ? kx : -kx];
+    if (DIM > 1) {
+      const int iy = (int)((i / ms0) % ms1);
+      const int ky = mode_of(iy, ms1, modeord);
+      g += (int64_t)nf0 * (ky >= 0 ? ky : nf1 + ky);
+      f *= i1[ky >= 0 ? ky : -ky];
+    }
+    if (DIM > 2) {
+      const int iz = (int)(i / ((int64_t)ms0 * ms1));
+      const int kz = mode_of(iz, ms2, modeord);
+      g += (int64_t)nf0 * nf1 * (kz >= 0 ? kz : nf2 + kz);
+      f *= i2[kz >= 0 ? kz : -kz];
+    }
+    const cplx<T> v = fw[(int64_t)tr * nf_total + g];
+    cplx<T> r;
+    r.x = v.x * f;
+    r.y = v.y * f;
+    fk[q] = r;
+  }
+}
+
+template <typename T, int DIM>
+__global__ void amplify_kernel(int ms0, int ms1, int ms2, int nf0, int nf1, int nf2, int modeord,
+                               const T *__restrict__ i0, const T *__restrict__ i1,
+                               const T *__restrict__ i2, const cplx<T> *__restrict__ fk,
+                               int64_t nmodes, cplx<T> *__restrict__ fw, int64_t nf_total,
+                               int ntr) {
+  const int64_t total = nf_total * ntr;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int tr = (int)(q / nf_total);
+    const int64_t g = q - (int64_t)tr * nf_total;
+    cplx<T> r;
+    r.x = T(0);
+    r.y = T(0);
+    bool in = true;
+    const int gx = (int)(g % nf0);
+    int kx = gx <= (ms0 - 1) / 2 ? gx : (gx >= nf0 - ms0 / 2 ? gx - nf0 : INT32_MIN);
+    in = kx != INT32_MIN;
+    int ky = 0, kz = 0;
+    if (DIM > 1 && in) {
+      const int gy = (int)((g / nf0) % nf1);
+      ky = gy <= (ms1 - 1) / 2 ? gy : (gy >= nf1 - ms1 / 2 ? gy - nf1 : INT32_MIN);
+      in = ky != INT32_MIN;
+    }
+    if (DIM > 2 && in) {
+      const int gz = (int)(g / ((int64_t)nf0 * nf1));
+      kz = gz <= (ms2 - 1) / 2 ? gz : (gz >= nf2 - ms2 / 2 ? gz - nf2 : INT32_MIN);
+      in = kz != INT32_MIN;
+    }
+    if (in) {
+      int64_t i = pos_of(kx, ms0, modeord);
+      T f = i0[kx >= 0 ? kx : -kx];
+      if (DIM > 1) {
+        i += (int64_t)ms0 * pos_of(ky, ms1, modeord);
+        f *= i1[ky >= 0 ? ky : -ky];
+      }
+      if (DIM > 2) {
+        i += (int64_t)ms0 * ms1 * pos_of(kz, ms2, modeord);
+        f *= i2[kz >= 0 ? kz : -kz];
+      }
+      const cplx<T> v = fk[(int64_t)tr * nmodes + i];
+      r.x = v.x * f;
+      r.y = v.y * f;
+    }
+    fw[q] = r;
+  }
+}
+
+template <typename T>
+__global__ void range_kernel(const T *__restrict__ a, int n, double *__restrict__ out) {
+  double lo = INFINITY, hi = -INFINITY;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = (double)a[i];
+    lo = fmin(lo, v);
+    hi = fmax(hi, v);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_down_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_down_sync(0xffffffffu, hi, o));
+  }
+  __shared__ double slo[32], shi[32];
+  if ((threadIdx.x & 31) == 0) {
+    slo[threadIdx.x >> 5] = lo;
+    shi[threadIdx.x >> 5] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      lo = fmin(lo, slo[w]);
+      hi = fmax(hi, shi[w]);
+    }
+    out[2 * blockIdx.x] = lo;
+    out[2 * blockIdx.x + 1] = hi;
+  }
+}
+
+template <typename T>
+__global__ void t3_prephase_kernel(int dim, const T *__restrict__ x, const T *__restrict__ y,
+                                   const T *__restrict__ z, int M, double D0, double D1, double D2,
+                                   int isign, cplx<T> *__restrict__ pre) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x) {
+    double ph = D0 * (double)x[j];
+    if (dim > 1) ph += D1 * (double)y[j];
+    if (dim > 2) ph += D2 * (double)z[j];
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    cplx<T> r;
+    r.x = (T)cs;
+    r.y = (T)(isign * sn);
+    pre[j] = r;
+  }
+}
+
+template <typename T>
+__global__ void t3_post_kernel(int dim, const T *__restrict__ s, const T *__restrict__ t,
+                               const T *__restrict__ u, int N, double C0, double C1, double C2,
+                               double D0, double D1, double D2, double sc0, double sc1,
+                               double sc2, int isign, QuadNodes Q, cplx<T> *__restrict__ post) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
+    const double a[3] = {(double)s[k] - D0, dim > 1 ? (double)t[k] - D1 : 0.0,
+                         dim > 2 ? (double)u[k] - D2 : 0.0};
+    const double sc[3] = {sc0, sc1, sc2};
+    double phihat = 1.0;
+    for (int d = 0; d < dim; ++d) {
+      const double w = sc[d] * a[d];
+      double acc = 0.0;
+      for (int n = 0; n < Q.q; ++n) acc += Q.f[n] * 2.0 * cos(w * Q.z[n]);
+      phihat *= acc;
+    }
+    const double ph = C0 * a[0] + C1 * a[1] + C2 * a[2];
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    cplx<T> r;
+    r.x = (T)(cs / phihat);
+    r.y = (T)(isign * sn / phihat);
+    post[k] = r;
+  }
+}
+} // namespace
+
+template <typename T> void launch_inv_fseries(int nf, const QuadNodes &Q, T *inv, cudaStream_t s) {
+  inv_fseries_kernel<T><<<blocks_for(nf / 2 + 1, 256), 256, 0, s>>>(nf, Q, inv);
+  GBN_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_deconv(int dim, const int ms[3], const int nf[3], int modeord, const T *const inv[3],
+                   const cplx<T> *fw, int64_t nf_total, cplx<T> *fk, int ntr, cudaStream_t s) {
+  const int64_t nmodes = (int64_t)ms[0] * ms[1] * ms[2];
+  const unsigned g = blocks_for(nmodes * ntr, 256);
+  if (dim == 1)
+    deconv_kernel<T, 1><<<g, 256, 0, s>>>(ms[0], 1, 1, nf[0], 1, 1, modeord, inv[0], inv[0],
+                                          inv[0], fw, nf_total, fk, nmodes, ntr);
+  else if (dim == 2)
+    deconv_kernel<T, 2><<<g, 256, 0, s>>>(ms[0], ms[1], 1, nf[0], nf[1], 1, modeord, inv[0],
+                                          inv[1], inv[1], fw, nf_total, fk, nmodes, ntr);
+  else
+    deconv_kernel<T, 3><<<g, 256, 0, s>>>(ms[0], ms[1], ms[2], nf[0], nf[1], nf[2], modeord,
+                                          inv[0], inv[1], inv[2], fw, nf_total, fk, nmodes, ntr);
+  GBN_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_amplify(int dim, const int ms[3], const int nf[3], int modeord,
+                    const T *const inv[3], const cplx<T> *fk, cplx<T> *fw, int64_t nf_total,
+                    int ntr, cudaStream_t s) {
+  const int64_t nmodes = (int64_t)ms[0] * ms[1] * ms[2];
+  const unsigned g = blocks_for(nf_total * ntr, 256);
+  if (dim == 1)
+    amplify_kernel<T, 1><<<g, 256, 0, s>>>(ms[0], 1, 1, nf[0], 1, 1, modeord, inv[0], inv[0],
+                                           inv[0], fk, nmodes, fw, nf_total, ntr);
+  else if (dim == 2)
+    amplify_kernel<T, 2><<<g, 256, 0, s>>>(ms[0], ms[1], 1, nf[0], nf[1], 1, modeord, inv[0],
+                                           inv[1], inv[1], fk, nmodes, fw, nf_total, ntr);
+  else
+    amplify_kernel<T, 3><<<g, 256, 0, s>>>(ms[0], ms[1], ms[2], nf[0], nf[1], nf[2], modeord,
+                                           inv[0], inv[1], inv[2], fk, nmodes, fw, nf_total, ntr);
+  GBN_LAUNCH_CHECK();
+}
+
+template <typename T> void array_range(const T *a, int n, double *lo, double *hi, cudaStream_t s) {
+  const int blocks = 256;
+  double *d = nullptr;
+  GBN_CUDA(cudaMallocAsync((void **)&d, 2 * blocks * sizeof(double), s));
+  range_kernel<T><<<blocks, 256, 0, s>>>(a, n, d);
+  GBN_LAUNCH_CHECK();
+  std::vector<double> h(2 * blocks);
+  GBN_CUDA(cudaMemcpyAsync(h.data(), d, 2 * blocks * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GBN_CUDA(cudaFreeAsync(d, s));
+  GBN_CUDA(cudaStreamSynchronize(s));
+  double l = INFINITY, u = -INFINITY;
+  for (int b = 0; b < blocks; ++b) {
+    l = std::fmin(l, h[2 * b]);
+    u = std::fmax(u, h[2 * b + 1]);
+  }
+  *lo = l;
+  *hi = u;
+}
+
+template <typename T>
+void launch_t3_prephase(int dim, const T *const xyz[3], int M, const double D[3], int isign,
+                        cplx<T> *pre, cudaStream_t s) {
+  if (M <= 0) return;
+  t3_prephase_kernel<T><<<blocks_for(M, 256), 256, 0, s>>>(
+      dim, xyz[0], dim > 1 ? xyz[1] : xyz[0], dim > 2 ? xyz[2] : xyz[0], M, D[0], D[1], D[2],
+      isign, pre);
+  GBN_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_t3_postfactor(int dim, const T *const stu[3], int N, const double C[3],
+                          const double D[3], const double scale[3], int isign,
+                          const QuadNodes &Q, cplx<T> *post, cudaStream_t s) {
+  if (N <= 0) return;
+  t3_post_kernel<T><<<blocks_for(N, 256), 256, 0, s>>>(
+      dim, stu[0], dim > 1 ? stu[1] : stu[0], dim > 2 ? stu[2] : stu[0], N, C[0], C[1], C[2],
+      D[0], D[1], D[2], scale[0], scale[1], scale[2], isign, Q, post);
+  GBN_LAUNCH_CHECK();
+}
+
+namespace {
+// Conflict-free shared-memory f32 atomicAdd loop: each warp adds into 32
+// consecutive words, so one instruction touches 32 distinct banks.
+__global__ void smem_atomic_probe(float *out, int iters) {
+  __shared__ float s[8192];
+  for (int i = threadIdx.x; i < 8192; i += blockDim.x) s[i] = 0.f;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const float v = 1.0f + threadIdx.x * 1e-3f;
+#pragma unroll 4
+  for (int it = 0; it < iters; ++it) atomicAdd(&s[(((it * 8 + w) * 32) & 8191) + lane], v);
+  __syncthreads();
+  if (threadIdx.x == 0) out[blockIdx.x] = s[blockIdx.x & 8191];
+}
+} // namespace
+
+double smem_atomic_rate(int device) {
+  int sms = 0;
+  GBN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const int grid = sms * 8, iters = 1 << 14;
+  float *d = nullptr;
+  GBN_CUDA(cudaMalloc(&d, (size_t)grid * sizeof(float)));
+  cudaEvent_t a, b;
+  GBN_CUDA(cudaEventCreate(&a));
+  GBN_CUDA(cudaEventCreate(&b));
+  smem_atomic_probe<<<grid, 256>>>(d, iters); // warm-up
+  GBN_CUDA(cudaEventRecord(a));
+  smem_atomic_probe<<<grid, 256>>>(d, iters);
+  GBN_CUDA(cudaEventRecord(b));
+  GBN_CUDA(cudaEventSynchronize(b));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(d);
+  return (double)grid * 256.0 * iters / (ms * 1e-3);
+}
+
+#define GBN_INST(T)                                                                            \
+  template void launch_inv_fseries<T>(int, const QuadNodes &, T *, cudaStream_t);            \
+  template void launch_deconv<T>(int, const int[3], const int[3], int, const T *const[3],   \
+                                 const cplx<T> *, int64_t, cplx<T> *, int, cudaStream_t);    \
+  template void launch_amplify<T>(int, const int[3], const int[3], int, const T *const[3],  \
+                                  const cplx<T> *, cplx<T> *, int64_t, int, cudaStream_t);   \
+  template void array_range<T>(const T *, int, double *, double *, cudaStream_t);           \
+  template void launch_t3_prephase<T>(int, const T *const[3], int, const double[3], int,    \
+                                      cplx<T> *, cudaStream_t);                              \
+  template void launch_t3_postfactor<T>(int, const T *const[3], int, const double[3],       \
+                                        const double[3], const double[3], int,              \
+                                        const QuadNodes &, cplx<T> *, cudaStream_t);
+GBN_INST(float)
+GBN_INST(double)
+
+} // namespace gbn

@@ -1,0 +1,447 @@
+// NUFFT plan orchestration: makeplan, setpts, execute (types 1, 2, 3), adjoint.
+//
+// Stage order follows the reference GPU library (src/cuda/makeplan.cu:223-398,
+// src/cuda/setpts.cu:25-314, src/cuda/execute.cu:105-258); buffers are sized at
+// plan/setpts time so execute allocates nothing and can be captured in a CUDA graph.
+#include "plan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+#include "planning.h"
+#include "sort.h"
+
+namespace gbn {
+
+DeviceScope::DeviceScope(int dev) {
+  GBN_CUDA(cudaGetDevice(&prev));
+  if (dev != prev) {
+    GBN_CUDA(cudaSetDevice(dev));
+    switched = true;
+  }
+}
+DeviceScope::~DeviceScope() {
+  if (switched) cudaSetDevice(prev);
+}
+
+namespace {
+int max_smem_optin(int dev) {
+  int v = 0;
+  GBN_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  return v;
+}
+int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+} // namespace
+
+template <typename T>
+Plan<T>::Plan(int type_, int dim_, const int64_t *modes_in, int iflag_, int ntransf_,
+              double tol_, const cufinufft_opts &opts_)
+    : type(type_), dim(dim_), ntransf(ntransf_), iflag(iflag_ >= 0 ? 1 : -1), batchsize(1),
+      tol(tol_), opts(opts_) {
+  if (dim < 1 || dim > 3) GBN_THROW(FINUFFT_ERR_DIM_NOTVALID, "dim");
+  DeviceScope ds(opts.gpu_device_id);
+  if (type < 1 || type > 3) {
+    fprintf(stderr, "[gbnufft] invalid type (%d): should be 1, 2, or 3\n", type);
+    GBN_THROW(FINUFFT_ERR_TYPE_NOTVALID, "type");
+  }
+  if (ntransf < 1) {
+    fprintf(stderr, "[gbnufft] invalid ntransf (%d): should be at least 1\n", ntransf);
+    GBN_THROW(FINUFFT_ERR_NTRANS_NOTVALID, "ntransf");
+  }
+  if (opts.gpu_method < 0 || opts.gpu_method > 4) GBN_THROW(FINUFFT_ERR_METHOD_NOTVALID, "method");
+  if (opts.gpu_method == 4 && dim != 3) GBN_THROW(FINUFFT_ERR_METHOD_NOTVALID, "method 4 is 3D only");
+  stream = (cudaStream_t)opts.gpu_stream;
+  if (type == 3) opts.gpu_spreadinterponly = 1; // the outer type 1 only spreads
+  else
+    for (int d = 0; d < dim; ++d) ms[d] = (int)modes_in[d];
+  nmodes = (int64_t)ms[0] * ms[1] * ms[2];
+  batchsize = opts.gpu_maxbatchsize > 0 ? opts.gpu_maxbatchsize : std::min(ntransf, 8);
+  if (type == 3) batchsize = std::min(batchsize, ntransf);
+  if (opts.upsampfac == 0.0) {
+    opts.upsampfac = 2.0;
+    if (type == 3 && tol >= 1e-9) opts.upsampfac = 1.25;
+  }
+  const bool is_float = std::is_same_v<T, float>;
+  const KernelChoice kc = choose_kernel(tol, opts.upsampfac, opts.gpu_kerevalmeth, is_float,
+                                        opts.gpu_spreadinterponly, opts.debug);
+  std::memset(&K, 0, sizeof(K));
+  K.ns = kc.ns;
+  K.beta = (T)kc.beta;
+  K.es_c = (T)(4.0 / (double(kc.ns) * kc.ns));
+  K.use_horner = opts.gpu_kerevalmeth == 1 ? 1 : 0;
+  {
+    // Horner pieces are fitted for any sigma; the reference only carries tables
+    // for sigma 2 and 1.25, which the option check above already enforces.
+    std::vector<double> coef;
+    const double target = std::max(1e-2 * tol, is_float ? 2e-7 : 4e-15);
+    const int H = horner_len(kc.ns);
+    const int ncoef = horner_fit(kc.ns, kc.beta, target, H, coef, &horner_err);
+    K.ncoef = H;
+    for (int k = 0; k < H; ++k)
+      for (int j = 0; j < kc.ns; ++j) {
+        const int src = k - (H - ncoef); // zero-pad the high-degree end
+        K.coef[k][j] = src >= 0 ? (T)coef[(size_t)src * MAX_NS + j] : T(0);
+      }
+    if (ncoef > H) K.use_horner = 0; // (cannot happen: fit is capped at MAX_HCOEF)
+  }
+  if (type != 3) {
+    for (int d = 0; d < dim; ++d)
+      nf[d] = opts.gpu_spreadinterponly ? ms[d]
+                                        : (int)fine_grid_len(ms[d], opts.upsampfac, K.ns);
+    nf_total = (int64_t)nf[0] * nf[1] * nf[2];
+    choose_spread_config(opts.gpu_method != 0);
+    if (!opts.gpu_spreadinterponly) {
+      fw.resize((size_t)nf_total * batchsize);
+      make_fft();
+      make_fseries();
+    }
+  }
+  if (opts.debug)
+    printf("[gbnufft] type %d dim %d ntr %d: ns=%d beta=%.4g sigma=%.3g nf=(%d,%d,%d) "
+           "method=%d bins=(%d,%d,%d) batch=%d horner_err=%.2e\n",
+           type, dim, ntransf, K.ns, (double)K.beta, opts.upsampfac, nf[0], nf[1], nf[2],
+           method, bins[0], bins[1], bins[2], batchsize, horner_err);
+}
+
+template <typename T> Plan<T>::~Plan() {
+  try {
+    DeviceScope ds(opts.gpu_device_id);
+    if (have_fft) cufftDestroy(fftplan);
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+  } catch (...) {
+  }
+}
+
+template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
+  // bins: user value, else a default of this engine per dimension and width
+  const int ns = K.ns;
+  int def = 1024;
+  if (dim == 2) def = 32;
+  if (dim == 3) {
+    const int tile = (std::is_same_v<T, float> ? (ns <= 8 ? 16 : 24) : (ns <= 8 ? 16 : 20));
+    def = std::max(4, tile - ns);
+  }
+  bins[0] = opts.gpu_binsizex > 0 ? opts.gpu_binsizex : def;
+  bins[1] = dim > 1 ? (opts.gpu_binsizey > 0 ? opts.gpu_binsizey : def) : 1;
+  bins[2] = dim > 2 ? (opts.gpu_binsizez > 0 ? opts.gpu_binsizez : def) : 1;
+  for (int d = 0; d < 3; ++d) {
+    if (d >= dim) bins[d] = 1;
+    nbins[d] = d < dim ? ceil_div(nf[d], bins[d]) : 1;
+  }
+  if (opts.gpu_maxsubprobsize < 1) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "maxsubprobsize");
+  method = opts.gpu_method == 0 ? 2 : (opts.gpu_method == 1 ? 1 : 2);
+  spread_smem = spread_tile_smem<T>(dim, ns, bins);
+  const int limit = max_smem_optin(opts.gpu_device_id);
+  if (method == 2 && spread_smem > (size_t)limit) {
+    if (user_method) {
+      fprintf(stderr, "[gbnufft] tile needs %zu bytes of shared memory, %d available\n",
+              spread_smem, limit);
+      GBN_THROW(FINUFFT_ERR_INSUFFICIENT_SHMEM, "tile too large");
+    }
+    method = 1;
+  }
+  scfg.method = method;
+  scfg.threads = 256;
+  scfg.smem = method == 2 ? spread_smem : 0;
+}
+
+template <typename T> void Plan<T>::make_fft() {
+  long long n[3];
+  for (int d = 0; d < dim; ++d) n[d] = nf[dim - 1 - d]; // slowest dimension first
+  size_t work = 0;
+  if (cufftCreate(&fftplan) != CUFFT_SUCCESS) GBN_THROW(FINUFFT_ERR_CUDA_FAILURE, "cufftCreate");
+  have_fft = true;
+  const cufftType ty = std::is_same_v<T, float> ? CUFFT_C2C : CUFFT_Z2Z;
+  cufftResult r = cufftMakePlanMany64(fftplan, dim, n, nullptr, 1, nf_total, nullptr, 1,
+                                      nf_total, ty, batchsize, &work);
+  if (r != CUFFT_SUCCESS) {
+    fprintf(stderr, "[gbnufft] cufftMakePlanMany64 failed (%d)\n", (int)r);
+    GBN_THROW(r == CUFFT_ALLOC_FAILED ? FINUFFT_ERR_ALLOC : FINUFFT_ERR_CUDA_FAILURE, "cufft");
+  }
+  cufftSetStream(fftplan, stream);
+}
+
+template <typename T> void Plan<T>::make_fseries() {
+  QuadNodes Q;
+  Q.q = kernel_ft_nodes(K.ns, (double)K.beta, 3.0, Q.z, Q.f);
+  for (int d = 0; d < dim; ++d) {
+    invphihat[d].resize((size_t)nf[d] / 2 + 1);
+    launch_inv_fseries<T>(nf[d], Q, invphihat[d].p, stream);
+  }
+}
+
+template <typename T> PointLayout<T> Plan<T>::layout() const {
+  PointLayout<T> L;
+  L.dim = dim;
+  for (int d = 0; d < 3; ++d) {
+    L.nf[d] = nf[d];
+    L.bin[d] = bins[d];
+    L.nbin[d] = nbins[d];
+    L.loc[d] = loc[d].p ? loc[d].p : loc[0].p;
+  }
+  L.M = M;
+  L.nsub = nsub;
+  L.sub_bin = sub_bin_.p;
+  L.sub_start = sub_start_.p;
+  L.sub_count = sub_count_.p;
+  L.perm = perm.p;
+  return L;
+}
+
+template <typename T>
+void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]) {
+  M = (int)Mp;
+  perm.resize(std::max<int64_t>(Mp, 1));
+  for (int d = 0; d < dim; ++d) loc[d].resize(std::max<int64_t>(Mp, 1));
+  const int nb = nbins[0] * nbins[1] * nbins[2];
+  int keybits = 0;
+  while ((1LL << keybits) < nb) ++keybits;
+  AsyncBuf keys((size_t)std::max<int64_t>(Mp, 1) * 4, stream);
+  AsyncBuf skeys((size_t)std::max<int64_t>(Mp, 1) * 4, stream);
+  if (M > 0) {
+    launch_bin_keys<T>(dim, xyz, M, ax, nbins, keys.as<uint32_t>(), stream);
+    stable_sort_by_bin(keys.as<uint32_t>(), M, keybits, skeys.as<uint32_t>(), perm.p, stream);
+    T *const lp[3] = {loc[0].p, dim > 1 ? loc[1].p : loc[0].p, dim > 2 ? loc[2].p : loc[0].p};
+    launch_sorted_local<T>(dim, xyz, perm.p, M, ax, lp, stream);
+  }
+  SubproblemArrays sa;
+  nsub = build_subproblems(skeys.as<uint32_t>(), M, nb, opts.gpu_maxsubprobsize, &sa, stream);
+  sub_bin_.release();
+  sub_start_.release();
+  sub_count_.release();
+  sub_bin_.p = sa.bin;
+  sub_start_.p = sa.start;
+  sub_count_.p = sa.count;
+  sub_bin_.n = sub_start_.n = sub_count_.n = (size_t)std::max(nsub, 1);
+}
+
+template <typename T>
+void Plan<T>::setpts(int64_t Mp, const T *x, const T *y, const T *z, int64_t Np, const T *s,
+                     const T *t, const T *u) {
+  DeviceScope ds(opts.gpu_device_id);
+  if (Mp < 0 || Mp > std::numeric_limits<int32_t>::max())
+    GBN_THROW(FINUFFT_ERR_NDATA_NOTVALID, "M");
+  const T *xyz[3] = {x, dim > 1 ? y : x, dim > 2 ? z : x};
+  if (Mp > 0 && (!x || (dim > 1 && !y) || (dim > 2 && !z)))
+    GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "null coordinate array");
+  if (type != 3) {
+    AxisMap ax[3];
+    for (int d = 0; d < 3; ++d) ax[d] = AxisMap{0.0, 1.0, nf[d], bins[d]};
+    sort_points(Mp, xyz, ax);
+    pts_set = true;
+    return;
+  }
+  // ---- type 3: choose the grid from the extents of sources and targets
+  if (Np < 0 || Np > std::numeric_limits<int32_t>::max()) {
+    fprintf(stderr, "[gbnufft] invalid number of targets N=%lld\n", (long long)Np);
+    GBN_THROW(FINUFFT_ERR_NUM_NU_PTS_INVALID, "N");
+  }
+  if (!s || (dim > 1 && !t) || (dim > 2 && !u)) {
+    fprintf(stderr, "[gbnufft] type 3 needs target arrays for every dimension\n");
+    GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "null target array");
+  }
+  N = (int)Np;
+  const T *stu[3] = {s, dim > 1 ? t : s, dim > 2 ? u : s};
+  for (int d = 0; d < 3; ++d) {
+    t3X[d] = t3C[d] = t3S[d] = t3D[d] = 0.0;
+    if (d >= dim) continue;
+    double lo, hi;
+    if (Mp > 0) {
+      array_range<T>(xyz[d], (int)Mp, &lo, &hi, stream);
+      width_center(lo, hi, &t3X[d], &t3C[d]);
+    }
+    if (Np > 0) {
+      array_range<T>(stu[d], (int)Np, &lo, &hi, stream);
+      width_center(lo, hi, &t3S[d], &t3D[d]);
+    }
+  }
+  int64_t nft[3] = {1, 1, 1};
+  for (int d = 0; d < dim; ++d) {
+    type3_grid(opts.upsampfac, t3X[d], t3S[d], K.ns, &nft[d], &t3h[d], &t3gam[d]);
+    if (nft[d] > std::numeric_limits<int32_t>::max()) GBN_THROW(FINUFFT_ERR_MAXNALLOC, "nf");
+    nf[d] = (int)nft[d];
+  }
+  nf_total = (int64_t)nf[0] * nf[1] * nf[2];
+  if (nf_total * batchsize > std::numeric_limits<int32_t>::max()) {
+    fprintf(stderr, "[gbnufft] type-3 fine grid batch would exceed %d cells\n",
+            std::numeric_limits<int32_t>::max());
+    GBN_THROW(FINUFFT_ERR_MAXNALLOC, "nf*batch");
+  }
+  if (opts.debug)
+    for (int d = 0; d < dim; ++d)
+      printf("[gbnufft] t3 dim %d: X=%.3g C=%.3g S=%.3g D=%.3g gam=%.4g nf=%d h=%.3g\n", d,
+             t3X[d], t3C[d], t3S[d], t3D[d], t3gam[d], nf[d], t3h[d]);
+  choose_spread_config(opts.gpu_method != 0);
+  // pre-phase exp(i isign D.x) (skipped when D = 0) and the post factor
+  const bool needpre = t3D[0] != 0.0 || t3D[1] != 0.0 || t3D[2] != 0.0;
+  if (needpre && Mp > 0) {
+    t3pre.resize((size_t)Mp);
+    launch_t3_prephase<T>(dim, xyz, (int)Mp, t3D, iflag, t3pre.p, stream);
+  } else
+    t3pre.release();
+  double scale[3];
+  for (int d = 0; d < 3; ++d) scale[d] = t3h[d] * t3gam[d];
+  QuadNodes Q;
+  Q.q = kernel_ft_nodes(K.ns, (double)K.beta, 2.0, Q.z, Q.f);
+  double Cphase[3] = {0, 0, 0};
+  for (int d = 0; d < dim; ++d)
+    if (std::isfinite(t3C[d])) Cphase[d] = t3C[d];
+  t3post.resize((size_t)std::max<int64_t>(Np, 1));
+  launch_t3_postfactor<T>(dim, stu, (int)Np, Cphase, t3D, scale, iflag, Q, t3post.p, stream);
+  // sort the rescaled sources x' = (x - C)/gamma on the outer grid
+  AxisMap ax[3];
+  for (int d = 0; d < 3; ++d)
+    ax[d] = AxisMap{d < dim ? t3C[d] : 0.0, d < dim ? 1.0 / t3gam[d] : 1.0, nf[d], bins[d]};
+  sort_points(Mp, xyz, ax);
+  fw.resize((size_t)nf_total * batchsize);
+  // inner type 2 on the outer grid, evaluated at s' = h gamma (s - D)
+  cufinufft_opts io = opts;
+  io.gpu_spreadinterponly = 0;
+  io.gpu_method = 0;
+  io.modeord = 0;
+  io.gpu_maxbatchsize = batchsize;
+  io.gpu_binsizex = io.gpu_binsizey = io.gpu_binsizez = 0;
+  int64_t inner_modes[3] = {nf[0], nf[1], nf[2]};
+  inner.reset();
+  inner.reset(new Plan<T>(2, dim, inner_modes, iflag, batchsize, tol, io));
+  AxisMap iax[3];
+  for (int d = 0; d < 3; ++d)
+    iax[d] = AxisMap{d < dim ? t3D[d] : 0.0, d < dim ? scale[d] : 1.0, inner->nf[d],
+                     inner->bins[d]};
+  inner->sort_points(Np, stu, iax);
+  inner->pts_set = true;
+  pts_set = true;
+}
+
+template <typename T> void Plan<T>::check_ready() const {
+  if (!pts_set) {
+    fprintf(stderr, "[gbnufft] execute called before setpts\n");
+    GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "setpts first");
+  }
+}
+
+template <typename T> void Plan<T>::fft(cplx<T> *data, int sign) {
+  const int dir = sign > 0 ? CUFFT_INVERSE : CUFFT_FORWARD;
+  cufftResult r;
+  if constexpr (std::is_same_v<T, float>)
+    r = cufftExecC2C(fftplan, (cufftComplex *)data, (cufftComplex *)data, dir);
+  else
+    r = cufftExecZ2Z(fftplan, (cufftDoubleComplex *)data, (cufftDoubleComplex *)data, dir);
+  if (r != CUFFT_SUCCESS) GBN_THROW(FINUFFT_ERR_CUDA_FAILURE, "cufftExec");
+}
+
+// Type-1 pipeline on ntr transforms: spread -> FFT(sign) -> deconvolve.
+template <typename T>
+void Plan<T>::run_type1(const cplx<T> *c, cplx<T> *fk, int ntr, int sign, const cplx<T> *pre,
+                        int conj_pre) {
+  const PointLayout<T> L = layout();
+  const T *inv[3] = {invphihat[0].p, dim > 1 ? invphihat[1].p : invphihat[0].p,
+                     dim > 2 ? invphihat[2].p : invphihat[0].p};
+  for (int i = 0; i * batchsize < ntr; ++i) {
+    const int blk = std::min(ntr - i * batchsize, batchsize);
+    const cplx<T> *cb = c + (int64_t)i * batchsize * M;
+    cplx<T> *fkb = fk + (int64_t)i * batchsize * nmodes;
+    cplx<T> *grid = opts.gpu_spreadinterponly ? fkb : fw.p;
+    if (time_stages) GBN_CUDA(cudaEventRecord(ev[0], stream));
+    GBN_CUDA(cudaMemsetAsync(grid, 0, (size_t)blk * nf_total * sizeof(cplx<T>), stream));
+    launch_spread<T>(L, K, cb, pre, conj_pre, grid, nf_total, blk, scfg, stream);
+    if (time_stages) GBN_CUDA(cudaEventRecord(ev[1], stream));
+    if (opts.gpu_spreadinterponly) continue;
+    fft(fw.p, sign);
+    if (time_stages) GBN_CUDA(cudaEventRecord(ev[2], stream));
+    launch_deconv<T>(dim, ms, nf, opts.modeord, inv, fw.p, nf_total, fkb, blk, stream);
+    if (time_stages) GBN_CUDA(cudaEventRecord(ev[3], stream));
+  }
+}
+
+// Type-2 pipeline on ntr transforms: amplify -> FFT(sign) -> interpolate.
+template <typename T>
+void Plan<T>::run_type2(const cplx<T> *fk, cplx<T> *c, int ntr, int sign,
+                        const cplx<T> *post, int conj_post) {
+  const PointLayout<T> L = layout();
+  const T *inv[3] = {invphihat[0].p, dim > 1 ? invphihat[1].p : invphihat[0].p,
+                     dim > 2 ? invphihat[2].p : invphihat[0].p};
+  for (int i = 0; i * batchsize < ntr; ++i) {
+    const int blk = std::min(ntr - i * batchsize, batchsize);
+    const cplx<T> *fkb = fk + (int64_t)i * batchsize * nmodes;
+    cplx<T> *cb = c + (int64_t)i * batchsize * M;
+    const cplx<T> *grid = fkb;
+    if (time_stages) GBN_CUDA(cudaEventRecord(ev[0], stream));
+    if (!opts.gpu_spreadinterponly) {
+      launch_amplify<T>(dim, ms, nf, opts.modeord, inv, fkb, fw.p, nf_total, blk, stream);
+      if (time_stages) GBN_CUDA(cudaEventRecord(ev[1], stream));
+      fft(fw.p, sign);
+      grid = fw.p;
+    } else if (time_stages)
+      GBN_CUDA(cudaEventRecord(ev[1], stream));
+    if (time_stages) GBN_CUDA(cudaEventRecord(ev[2], stream));
+    launch_interp<T>(L, K, grid, nf_total, post, conj_post, cb, blk, stream);
+    if (time_stages) GBN_CUDA(cudaEventRecord(ev[3], stream));
+  }
+}
+
+template <typename T> void Plan<T>::execute(cplx<T> *c, cplx<T> *fk) {
+  DeviceScope ds(opts.gpu_device_id);
+  check_ready();
+  if (time_stages)
+    for (auto &e : ev)
+      if (!e) GBN_CUDA(cudaEventCreate(&e));
+  if (type == 1) run_type1(c, fk, ntransf, iflag, nullptr, 0);
+  else if (type == 2) run_type2(fk, c, ntransf, iflag, nullptr, 0);
+  else {
+    // type 3: pre-phase+spread onto the outer grid, inner type 2, post factor
+    const PointLayout<T> L = layout();
+    for (int i = 0; i * batchsize < ntransf; ++i) {
+      const int blk = std::min(ntransf - i * batchsize, batchsize);
+      const cplx<T> *cb = c + (int64_t)i * batchsize * M;
+      cplx<T> *fb = fk + (int64_t)i * batchsize * N;
+      GBN_CUDA(cudaMemsetAsync(fw.p, 0, (size_t)blk * nf_total * sizeof(cplx<T>), stream));
+      launch_spread<T>(L, K, cb, t3pre.p ? t3pre.p : nullptr, 0, fw.p, nf_total, blk, scfg,
+                       stream);
+      inner->run_type2(fw.p, fb, blk, iflag, t3post.p, 0);
+    }
+  }
+  GBN_LAUNCH_CHECK();
+  if (time_stages) {
+    GBN_CUDA(cudaEventSynchronize(ev[3]));
+    cudaEventElapsedTime(&times.spread_or_interp_ms, ev[0], ev[1]);
+    cudaEventElapsedTime(&times.fft_ms, ev[1], ev[2]);
+    cudaEventElapsedTime(&times.deconv_ms, ev[2], ev[3]);
+    cudaEventElapsedTime(&times.total_ms, ev[0], ev[3]);
+  }
+}
+
+// Adjoint of the planned transform (reference CPU semantics,
+// include/finufft/execute.hpp:318-357): type 1 -> type 2 with the opposite
+// sign (fk in, c out), type 2 -> type 1 with the opposite sign (c in, fk out),
+// type 3 -> the planned factors applied backwards and conjugated.
+template <typename T> void Plan<T>::execute_adjoint(cplx<T> *c, cplx<T> *fk) {
+  DeviceScope ds(opts.gpu_device_id);
+  check_ready();
+  const bool tmp_ts = time_stages;
+  time_stages = false;
+  if (type == 1) run_type2(fk, c, ntransf, -iflag, nullptr, 0);
+  else if (type == 2) run_type1(c, fk, ntransf, -iflag, nullptr, 0);
+  else {
+    const PointLayout<T> L = layout();
+    for (int i = 0; i * batchsize < ntransf; ++i) {
+      const int blk = std::min(ntransf - i * batchsize, batchsize);
+      cplx<T> *cb = c + (int64_t)i * batchsize * M;
+      const cplx<T> *fb = fk + (int64_t)i * batchsize * N;
+      // adjoint of (post * inner type 2): inner type 1 with conj(post) pre-factor
+      inner->run_type1(fb, fw.p, blk, -iflag, t3post.p, 1);
+      // adjoint of (spread * pre): interpolate, times conj(pre)
+      launch_interp<T>(L, K, fw.p, nf_total, t3pre.p ? t3pre.p : nullptr, 1, cb, blk, stream);
+    }
+  }
+  time_stages = tmp_ts;
+  GBN_LAUNCH_CHECK();
+}
+
+template class Plan<float>;
+template class Plan<double>;
+
+} // namespace gbn

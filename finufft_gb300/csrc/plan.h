@@ -1,0 +1,113 @@
+// The NUFFT plan: owns every device buffer of one transform set and runs the
+// makeplan -> setpts -> execute pipeline on one CUDA stream.
+#pragma once
+#include <cufft.h>
+
+#include <memory>
+#include <vector>
+
+#include "common.h"
+#include "cufinufft_opts.h"
+#include "device_util.cuh"
+#include "elementwise.h"
+#include "spreadinterp.h"
+
+namespace gbn {
+
+// Owning device buffer (cudaMalloc).
+template <typename U> struct DevArray {
+  U *p = nullptr;
+  size_t n = 0;
+  DevArray() = default;
+  DevArray(const DevArray &) = delete;
+  DevArray &operator=(const DevArray &) = delete;
+  ~DevArray() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void resize(size_t count) {
+    if (count == n && p) return;
+    release();
+    if (count) GBN_CUDA(cudaMalloc((void **)&p, count * sizeof(U)));
+    n = count;
+  }
+};
+
+// Makes opts.gpu_device_id current for a scope and restores the caller's device.
+struct DeviceScope {
+  int prev = 0;
+  bool switched = false;
+  explicit DeviceScope(int dev);
+  ~DeviceScope();
+};
+
+// Per-stage device timings of the last execute (milliseconds).
+struct StageTimes {
+  float spread_or_interp_ms = 0, fft_ms = 0, deconv_ms = 0, total_ms = 0;
+};
+
+template <typename T> class Plan {
+public:
+  Plan(int type, int dim, const int64_t *nmodes, int iflag, int ntransf, double tol,
+       const cufinufft_opts &opts);
+  ~Plan();
+  void setpts(int64_t M, const T *x, const T *y, const T *z, int64_t N, const T *s,
+              const T *t, const T *u);
+  void execute(cplx<T> *c, cplx<T> *fk);
+  void execute_adjoint(cplx<T> *c, cplx<T> *fk);
+
+  // introspection (tests, planner, benchmarks)
+  int type, dim, ntransf, iflag, batchsize;
+  double tol;
+  cufinufft_opts opts;
+  int ms[3] = {1, 1, 1};
+  int nf[3] = {1, 1, 1};
+  int64_t nf_total = 1, nmodes = 1;
+  int M = 0, N = 0;
+  KernelShape<T> K;
+  double horner_err = 0;
+  int method = 2;
+  int bins[3] = {1, 1, 1};
+  int nbins[3] = {1, 1, 1};
+  int nsub = 0;
+  size_t spread_smem = 0;
+  cudaStream_t stream = nullptr;
+  StageTimes times;
+  bool time_stages = false;
+  // sorted point layout (device)
+  DevArray<int> perm;
+  DevArray<T> loc[3];
+  DevArray<int> sub_bin_, sub_start_, sub_count_;
+  PointLayout<T> layout() const;
+
+  // type 3 parameters (per dimension)
+  double t3X[3] = {0, 0, 0}, t3C[3] = {0, 0, 0}, t3S[3] = {0, 0, 0}, t3D[3] = {0, 0, 0};
+  double t3h[3] = {1, 1, 1}, t3gam[3] = {1, 1, 1};
+  std::unique_ptr<Plan<T>> inner; // type 3: the type-2 plan on the outer grid
+
+private:
+  void choose_spread_config(bool user_method);
+  void make_fft();
+  void make_fseries();
+  void sort_points(int64_t M, const T *const xyz[3], const AxisMap ax[3]);
+  void run_type1(const cplx<T> *c, cplx<T> *fk, int ntr, int sign, const cplx<T> *pre,
+                 int conj_pre);
+  void run_type2(const cplx<T> *fk, cplx<T> *c, int ntr, int sign, const cplx<T> *post,
+                 int conj_post);
+  void fft(cplx<T> *data, int sign);
+  void check_ready() const;
+
+  cufftHandle fftplan = 0;
+  bool have_fft = false;
+  DevArray<cplx<T>> fw;        // batchsize fine grids
+  DevArray<T> invphihat[3];    // 1/phihat per dimension, nf/2+1 each
+  DevArray<cplx<T>> t3pre;     // type 3 pre-phase, M
+  DevArray<cplx<T>> t3post;    // type 3 post factor, N
+  bool pts_set = false;
+  SpreadConfig scfg{2, 256, 0};
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+} // namespace gbn

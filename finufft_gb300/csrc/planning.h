@@ -1,0 +1,47 @@
+// Host-side planning math: kernel width and shape, fine-grid sizes, quadrature
+// nodes, Horner fits and bin sizes. Pure C++, no CUDA calls.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+namespace gbn {
+
+// Smallest even 2,3,5-smooth integer >= n (FINUFFT's next235(n, 2)).
+int64_t next235_even(int64_t n);
+
+// n-node Gauss-Legendre rule on [-1,1]: nodes ascending, weights.
+void gauss_legendre(int n, double *x, double *w);
+
+// ES kernel width and beta for a requested tolerance (GPU library rule).
+struct KernelChoice {
+  int ns;
+  double beta;
+};
+// Throws Error(FINUFFT_ERR_HORNER_WRONG_BETA / UPSAMPFAC_TOO_SMALL) as the reference does.
+KernelChoice choose_kernel(double tol, double sigma, int kerevalmeth, int is_float,
+                           int spreadinterponly, int debug);
+
+// ES kernel value at x (grid units), support |x| < ns/2.
+double es_kernel(double x, int ns, double beta);
+
+// Fine grid length for a type 1/2 dimension with ms modes.
+int64_t fine_grid_len(int64_t ms, double sigma, int ns);
+
+// Type-3 grid: given source half-width X and frequency half-width S.
+void type3_grid(double sigma, double X, double S, int ns, int64_t *nf, double *h,
+                double *gam);
+
+// Half-width and centre of an interval [lo,hi], re-centring only when it pays.
+void width_center(double lo, double hi, double *w, double *c);
+
+// Horner fit of the ES kernel: fills coef[k*16 + j] (k = 0 highest degree),
+// returns the number of coefficients per piece (<= maxcoef) and the max abs error seen.
+int horner_fit(int ns, double beta, double target_err, int maxcoef, std::vector<double> &coef,
+               double *maxerr);
+
+// Quadrature nodes/weights for the kernel Fourier transform:
+//   phihat(k) = sum_n f[n] * 2 cos(k z[n]),  z in grid units.
+// q = number of nodes used.
+int kernel_ft_nodes(int ns, double beta, double nodes_per_halfwidth, double *z, double *f);
+
+} // namespace gbn

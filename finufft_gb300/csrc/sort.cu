@@ -1,0 +1,380 @@
+// setpts on the device: fold-rescale, bin keys, a stable LSD radix sort of the
+// points by bin, per-bin ranges and the subproblem table.
+//
+// The reference (include/cufinufft/spreadinterp.hpp:299-350,
+// src/cuda/spread_subprob_inst.cu:136-181) ranks points inside a bin with
+// global atomics, so its in-bin order changes from run to run. Here the sort is
+// stable: points of one bin keep their input order, which is exactly the
+// permutation a host counting sort produces (include/finufft/spread.hpp:459-584
+// for the CPU library's bin ordering: x fastest, then y, then z).
+#include "sort.h"
+
+namespace gbn {
+
+// ---------------------------------------------------------------- scan ----
+namespace {
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;
+
+__global__ void scan_block_sums(const int *__restrict__ in, int64_t n, int *__restrict__ sums) {
+  __shared__ int red[32];
+  const int64_t base = (int64_t)blockIdx.x * SCAN_CHUNK;
+  int s = 0;
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    int64_t i = base + (int64_t)j * SCAN_THREADS + threadIdx.x;
+    if (i < n) s += in[i];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = red[threadIdx.x];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) sums[blockIdx.x] = s;
+  }
+}
+
+__global__ void scan_chunks(const int *__restrict__ in, int64_t n,
+                            const int *__restrict__ chunk_off, int *__restrict__ out) {
+  __shared__ int wexcl[32];
+  __shared__ int wtot[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t base = (int64_t)blockIdx.x * SCAN_CHUNK + (int64_t)threadIdx.x * SCAN_ITEMS;
+  int v[SCAN_ITEMS];
+  int sum = 0;
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    int64_t i = base + j;
+    v[j] = (i < n) ? in[i] : 0;
+    sum += v[j];
+  }
+  // inclusive warp scan of thread sums
+  int x = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wtot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int s = wtot[lane];
+    int t = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    wexcl[lane] = t - s;
+  }
+  __syncthreads();
+  int run = (chunk_off ? chunk_off[blockIdx.x] : 0) + wexcl[w] + (x - sum);
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    int64_t i = base + j;
+    if (i < n) out[i] = run;
+    run += v[j];
+  }
+}
+} // namespace
+
+void exclusive_scan_i32(const int *in, int *out, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  const int64_t nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+  if (nb == 1) {
+    scan_chunks<<<1, SCAN_THREADS, 0, s>>>(in, n, nullptr, out);
+    GBN_LAUNCH_CHECK();
+    return;
+  }
+  AsyncBuf sums(nb * sizeof(int), s), offs(nb * sizeof(int), s);
+  scan_block_sums<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, sums.as<int>());
+  GBN_LAUNCH_CHECK();
+  exclusive_scan_i32(sums.as<int>(), offs.as<int>(), nb, s);
+  scan_chunks<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, offs.as<int>(), out);
+  GBN_LAUNCH_CHECK();
+}
+
+// ------------------------------------------------------------ bin keys ----
+namespace {
+template <typename T, int DIM>
+__global__ void bin_key_kernel(const T *__restrict__ x, const T *__restrict__ y,
+                               const T *__restrict__ z, int M, AxisMap a0, AxisMap a1,
+                               AxisMap a2, int nb0, int nb1, uint32_t *__restrict__ keys) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+    int c;
+    double f;
+    fold_cell((double)x[i], a0, c, f);
+    uint32_t key = (uint32_t)(c / a0.bin);
+    if (DIM > 1) {
+      fold_cell((double)y[i], a1, c, f);
+      key += (uint32_t)nb0 * (uint32_t)(c / a1.bin);
+    }
+    if (DIM > 2) {
+      fold_cell((double)z[i], a2, c, f);
+      key += (uint32_t)nb0 * (uint32_t)nb1 * (uint32_t)(c / a2.bin);
+    }
+    keys[i] = key;
+  }
+}
+
+template <typename T, int DIM>
+__global__ void sorted_local_kernel(const T *__restrict__ x, const T *__restrict__ y,
+                                    const T *__restrict__ z, const int *__restrict__ perm,
+                                    int M, AxisMap a0, AxisMap a1, AxisMap a2,
+                                    T *__restrict__ l0, T *__restrict__ l1,
+                                    T *__restrict__ l2) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < M; p += gridDim.x * blockDim.x) {
+    const int i = perm[p];
+    int c;
+    double f;
+    fold_cell((double)x[i], a0, c, f);
+    l0[p] = (T)((double)(c - (c / a0.bin) * a0.bin) + f);
+    if (DIM > 1) {
+      fold_cell((double)y[i], a1, c, f);
+      l1[p] = (T)((double)(c - (c / a1.bin) * a1.bin) + f);
+    }
+    if (DIM > 2) {
+      fold_cell((double)z[i], a2, c, f);
+      l2[p] = (T)((double)(c - (c / a2.bin) * a2.bin) + f);
+    }
+  }
+}
+
+inline unsigned grid_for(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b > 152 * 64) b = 152 * 64;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+} // namespace
+
+template <typename T>
+void launch_bin_keys(int dim, const T *const xyz[3], int M, const AxisMap ax[3],
+                     const int nbin[3], uint32_t *keys, cudaStream_t s) {
+  if (M <= 0) return;
+  const unsigned g = grid_for(M, 256);
+  if (dim == 1)
+    bin_key_kernel<T, 1><<<g, 256, 0, s>>>(xyz[0], xyz[0], xyz[0], M, ax[0], ax[0], ax[0],
+                                           nbin[0], 1, keys);
+  else if (dim == 2)
+    bin_key_kernel<T, 2><<<g, 256, 0, s>>>(xyz[0], xyz[1], xyz[1], M, ax[0], ax[1], ax[1],
+                                           nbin[0], nbin[1], keys);
+  else
+    bin_key_kernel<T, 3><<<g, 256, 0, s>>>(xyz[0], xyz[1], xyz[2], M, ax[0], ax[1], ax[2],
+                                           nbin[0], nbin[1], keys);
+  GBN_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_sorted_local(int dim, const T *const xyz[3], const int *perm, int M,
+                         const AxisMap ax[3], T *const loc[3], cudaStream_t s) {
+  if (M <= 0) return;
+  const unsigned g = grid_for(M, 256);
+  if (dim == 1)
+    sorted_local_kernel<T, 1><<<g, 256, 0, s>>>(xyz[0], xyz[0], xyz[0], perm, M, ax[0], ax[0],
+                                                ax[0], loc[0], loc[0], loc[0]);
+  else if (dim == 2)
+    sorted_local_kernel<T, 2><<<g, 256, 0, s>>>(xyz[0], xyz[1], xyz[1], perm, M, ax[0], ax[1],
+                                                ax[1], loc[0], loc[1], loc[1]);
+  else
+    sorted_local_kernel<T, 3><<<g, 256, 0, s>>>(xyz[0], xyz[1], xyz[2], perm, M, ax[0], ax[1],
+                                                ax[2], loc[0], loc[1], loc[2]);
+  GBN_LAUNCH_CHECK();
+}
+
+template void launch_bin_keys<float>(int, const float *const[3], int, const AxisMap[3],
+                                     const int[3], uint32_t *, cudaStream_t);
+template void launch_bin_keys<double>(int, const double *const[3], int, const AxisMap[3],
+                                      const int[3], uint32_t *, cudaStream_t);
+template void launch_sorted_local<float>(int, const float *const[3], const int *, int,
+                                         const AxisMap[3], float *const[3], cudaStream_t);
+template void launch_sorted_local<double>(int, const double *const[3], const int *, int,
+                                          const AxisMap[3], double *const[3], cudaStream_t);
+
+// --------------------------------------------------------- radix sort ----
+namespace {
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS; // 4096 keys per block
+constexpr int RS_WARP_SPAN = RS_TILE / RS_WARPS; // 512 consecutive keys per warp
+
+__global__ void radix_hist_kernel(const uint32_t *__restrict__ keys, int M, int shift,
+                                  int ntiles, int *__restrict__ hist) {
+  __shared__ int cnt[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) cnt[i] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * RS_TILE;
+#pragma unroll 4
+  for (int j = 0; j < RS_ITEMS; ++j) {
+    const int64_t i = base + (int64_t)j * RS_THREADS + threadIdx.x;
+    if (i < M) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < 256; d += blockDim.x)
+    hist[(int64_t)d * ntiles + blockIdx.x] = cnt[d];
+}
+
+// Stable scatter: rank of a key among equal digits of its tile follows index
+// order (warp 0's 512 keys, then warp 1's, ...; inside a warp 32 keys per step).
+__global__ void radix_scatter_kernel(const uint32_t *__restrict__ kin,
+                                     const int *__restrict__ vin, uint32_t *__restrict__ kout,
+                                     int *__restrict__ vout, int M, int shift, int ntiles,
+                                     const int *__restrict__ offs) {
+  __shared__ int wcnt[RS_WARPS][256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < RS_WARPS * 256; i += blockDim.x) (&wcnt[0][0])[i] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)w * RS_WARP_SPAN;
+  const unsigned lt = (1u << lane) - 1u;
+  uint32_t key[RS_ITEMS];
+  int rank[RS_ITEMS];
+#pragma unroll
+  for (int j = 0; j < RS_ITEMS; ++j) {
+    const int64_t i = base + j * 32 + lane;
+    const bool ok = i < M;
+    const uint32_t k = ok ? kin[i] : 0u;
+    const int d = ok ? (int)((k >> shift) & 255u) : 256;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    int r = 0;
+    if (ok) r = wcnt[w][d] + __popc(peers & lt);
+    __syncwarp();
+    if (ok && (peers & lt) == 0u) wcnt[w][d] += __popc(peers);
+    __syncwarp();
+    key[j] = k;
+    rank[j] = r;
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+    int run = 0;
+#pragma unroll
+    for (int ww = 0; ww < RS_WARPS; ++ww) {
+      const int t = wcnt[ww][d];
+      wcnt[ww][d] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < RS_ITEMS; ++j) {
+    const int64_t i = base + j * 32 + lane;
+    if (i < M) {
+      const int d = (int)((key[j] >> shift) & 255u);
+      const int pos = offs[(int64_t)d * ntiles + blockIdx.x] + wcnt[w][d] + rank[j];
+      kout[pos] = key[j];
+      vout[pos] = vin ? vin[i] : (int)i;
+    }
+  }
+}
+
+__global__ void iota_kernel(int *v, int M) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x)
+    v[i] = i;
+}
+} // namespace
+
+void stable_sort_by_bin(uint32_t *keys_in, int M, int keybits, uint32_t *keys_out,
+                        int *perm_out, cudaStream_t s) {
+  if (M <= 0) return;
+  const int passes = (keybits + 7) / 8;
+  if (passes == 0) { // single bin: identity permutation
+    iota_kernel<<<grid_for(M, 256), 256, 0, s>>>(perm_out, M);
+    GBN_LAUNCH_CHECK();
+    GBN_CUDA(cudaMemcpyAsync(keys_out, keys_in, (size_t)M * 4, cudaMemcpyDeviceToDevice, s));
+    return;
+  }
+  const int ntiles = (int)(((int64_t)M + RS_TILE - 1) / RS_TILE);
+  AsyncBuf hist((size_t)256 * ntiles * sizeof(int), s);
+  AsyncBuf offs((size_t)256 * ntiles * sizeof(int), s);
+  AsyncBuf ktmp((size_t)M * 4, s), vtmp((size_t)M * 4, s);
+  // ping-pong so the last pass lands in (keys_out, perm_out)
+  const uint32_t *ks = keys_in;
+  const int *vs = nullptr; // pass 0 uses the identity as values
+  for (int p = 0; p < passes; ++p) {
+    const bool to_out = ((passes - 1 - p) % 2) == 0;
+    uint32_t *kd = to_out ? keys_out : ktmp.as<uint32_t>();
+    int *vd = to_out ? perm_out : vtmp.as<int>();
+    const int shift = 8 * p;
+    radix_hist_kernel<<<ntiles, RS_THREADS, 0, s>>>(ks, M, shift, ntiles, hist.as<int>());
+    GBN_LAUNCH_CHECK();
+    exclusive_scan_i32(hist.as<int>(), offs.as<int>(), (int64_t)256 * ntiles, s);
+    radix_scatter_kernel<<<ntiles, RS_THREADS, 0, s>>>(ks, vs, kd, vd, M, shift, ntiles,
+                                                       offs.as<int>());
+    GBN_LAUNCH_CHECK();
+    ks = kd;
+    vs = vd;
+  }
+}
+
+// ----------------------------------------------------------- subproblems ----
+namespace {
+__global__ void bin_bounds_kernel(const uint32_t *__restrict__ sk, int M, int *__restrict__ bstart,
+                                  int *__restrict__ bend) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+    const uint32_t b = sk[i];
+    if (i == 0 || sk[i - 1] != b) bstart[b] = i;
+    if (i == M - 1 || sk[i + 1] != b) bend[b] = i + 1;
+  }
+}
+__global__ void bin_nsub_kernel(const int *__restrict__ bstart, int *__restrict__ bend_to_cnt,
+                                int *__restrict__ nsub, int nbins, int maxsub) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += gridDim.x * blockDim.x) {
+    const int cnt = bend_to_cnt[b] - bstart[b];
+    bend_to_cnt[b] = cnt;
+    nsub[b] = (cnt + maxsub - 1) / maxsub;
+  }
+}
+__global__ void fill_subproblems_kernel(const int *__restrict__ bstart, const int *__restrict__ bcnt,
+                                        const int *__restrict__ nsub,
+                                        const int *__restrict__ substart, int nbins, int maxsub,
+                                        int *__restrict__ sbin, int *__restrict__ sstart,
+                                        int *__restrict__ scount) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += gridDim.x * blockDim.x) {
+    const int n = nsub[b], o = substart[b], st = bstart[b], c = bcnt[b];
+    for (int k = 0; k < n; ++k) {
+      sbin[o + k] = b;
+      sstart[o + k] = st + k * maxsub;
+      scount[o + k] = min(maxsub, c - k * maxsub);
+    }
+  }
+}
+} // namespace
+
+int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, int maxsub,
+                      SubproblemArrays *out, cudaStream_t s) {
+  AsyncBuf bstart((size_t)nbins * 4, s), bcnt((size_t)nbins * 4, s), nsub((size_t)nbins * 4, s),
+      substart((size_t)nbins * 4, s);
+  GBN_CUDA(cudaMemsetAsync(bstart.p, 0, (size_t)nbins * 4, s));
+  GBN_CUDA(cudaMemsetAsync(bcnt.p, 0, (size_t)nbins * 4, s));
+  if (M > 0) {
+    bin_bounds_kernel<<<grid_for(M, 256), 256, 0, s>>>(sorted_keys, M, bstart.as<int>(),
+                                                       bcnt.as<int>());
+    GBN_LAUNCH_CHECK();
+  }
+  bin_nsub_kernel<<<grid_for(nbins, 256), 256, 0, s>>>(bstart.as<int>(), bcnt.as<int>(),
+                                                       nsub.as<int>(), nbins, maxsub);
+  GBN_LAUNCH_CHECK();
+  exclusive_scan_i32(nsub.as<int>(), substart.as<int>(), nbins, s);
+  int last[2] = {0, 0};
+  GBN_CUDA(cudaMemcpyAsync(&last[0], substart.as<int>() + nbins - 1, 4, cudaMemcpyDeviceToHost, s));
+  GBN_CUDA(cudaMemcpyAsync(&last[1], nsub.as<int>() + nbins - 1, 4, cudaMemcpyDeviceToHost, s));
+  GBN_CUDA(cudaStreamSynchronize(s));
+  const int total = last[0] + last[1];
+  if (out->bin) cudaFree(out->bin);
+  if (out->start) cudaFree(out->start);
+  if (out->count) cudaFree(out->count);
+  out->bin = out->start = out->count = nullptr;
+  const size_t nalloc = (size_t)(total > 0 ? total : 1) * 4;
+  GBN_CUDA(cudaMalloc(&out->bin, nalloc));
+  GBN_CUDA(cudaMalloc(&out->start, nalloc));
+  GBN_CUDA(cudaMalloc(&out->count, nalloc));
+  fill_subproblems_kernel<<<grid_for(nbins, 256), 256, 0, s>>>(
+      bstart.as<int>(), bcnt.as<int>(), nsub.as<int>(), substart.as<int>(), nbins, maxsub,
+      out->bin, out->start, out->count);
+  GBN_LAUNCH_CHECK();
+  return total;
+}
+
+} // namespace gbn

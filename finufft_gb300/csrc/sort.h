@@ -1,0 +1,52 @@
+// Device bin sort of nonuniform points (setpts stage).
+#pragma once
+#include <cstdint>
+#include "common.h"
+#include "device_util.cuh"
+
+namespace gbn {
+
+// Stream-ordered device scratch buffer (cudaMallocAsync / cudaFreeAsync).
+struct AsyncBuf {
+  void *p = nullptr;
+  cudaStream_t s = nullptr;
+  AsyncBuf() = default;
+  AsyncBuf(size_t bytes, cudaStream_t st) : s(st) {
+    if (bytes) GBN_CUDA(cudaMallocAsync(&p, bytes, st));
+  }
+  ~AsyncBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  AsyncBuf(const AsyncBuf &) = delete;
+  AsyncBuf &operator=(const AsyncBuf &) = delete;
+  template <typename U> U *as() const { return (U *)p; }
+};
+
+// Exclusive prefix sum of n int32 values (out may alias nothing of in).
+void exclusive_scan_i32(const int *in, int *out, int64_t n, cudaStream_t s);
+
+// Bin key of every point: bx + nb0*(by + nb1*bz) with x fastest.
+template <typename T>
+void launch_bin_keys(int dim, const T *const xyz[3], int M, const AxisMap ax[3],
+                     const int nbin[3], uint32_t *keys, cudaStream_t s);
+
+// Stable LSD radix sort of (key, index) pairs by the low `keybits` bits of key.
+// On return perm_out[p] is the user index of the p-th point in bin order and
+// keys_out[p] its bin. keys_in is clobbered.
+void stable_sort_by_bin(uint32_t *keys_in, int M, int keybits, uint32_t *keys_out,
+                        int *perm_out, cudaStream_t s);
+
+// Per-bin [start, count) of the sorted keys and subproblem decomposition.
+// Returns the number of subproblems (one device->host copy, stream sync).
+struct SubproblemArrays {
+  int *bin = nullptr, *start = nullptr, *count = nullptr;
+};
+int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, int maxsub,
+                      SubproblemArrays *out, cudaStream_t s);
+
+// Sorted bin-local coordinates loc[d][p] in [0, bin_d], grid units.
+template <typename T>
+void launch_sorted_local(int dim, const T *const xyz[3], const int *perm, int M,
+                         const AxisMap ax[3], T *const loc[3], cudaStream_t s);
+
+} // namespace gbn

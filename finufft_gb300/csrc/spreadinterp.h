@@ -1,0 +1,29 @@
+// Spread (type 1) and interpolation (type 2) kernel launchers.
+#pragma once
+#include "common.h"
+
+namespace gbn {
+
+struct SpreadConfig {
+  int method;       // 1: point-driven global atomics, 2: tiled shared memory
+  int threads;      // CTA size
+  size_t smem;      // dynamic shared memory bytes for method 2
+};
+
+// Shared-memory bytes of the tiled spread for a given tile and kernel width.
+template <typename T> size_t spread_tile_smem(int dim, int ns, const int bin[3]);
+
+// fw[t*nf + g] += sum_j c[t*M + j] (* pre[j] or conj(pre[j])) phi(g - x_j), t < ntr.
+// fw must be zeroed by the caller.
+template <typename T>
+void launch_spread(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *c,
+                   const cplx<T> *pre, int conj_pre, cplx<T> *fw, int64_t nf_total, int ntr,
+                   const SpreadConfig &cfg, cudaStream_t s);
+
+// out[t*M + j] = (post ? post[j] : 1) * sum_g fw[t*nf + g] phi(g - x_j), t < ntr.
+template <typename T>
+void launch_interp(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *fw,
+                   int64_t nf_total, const cplx<T> *post, int conj_post, cplx<T> *out, int ntr,
+                   cudaStream_t s);
+
+} // namespace gbn

@@ -1,0 +1,408 @@
+// Spreading and interpolation kernels, templated on precision, dimension and
+// kernel width. Included by one translation unit per dimension.
+//
+// Both work on subproblems: a run of at most maxsubprobsize bin-sorted points
+// that all fall in one bin, so their kernel supports lie in a tile of
+// (bin + ns) cells per dimension whose origin is the bin origin minus
+// floor(ns/2). A point's bin-local coordinate l is in [0, bin]; its first
+// support cell in tile coordinates is s = ceil(l - ns/2) + floor(ns/2) in
+// [0, bin] and its kernel weights are phi(ceil(l - ns/2) - l + j), j < ns.
+#pragma once
+#include "device_util.cuh"
+#include "spreadinterp.h"
+
+namespace gbn {
+
+template <int DIM> struct TileGeom {
+  int t[3];    // tile extent per dimension (bin + ns, 1 beyond DIM)
+  int org[3];  // global index of tile cell 0 per dimension (may be negative)
+  int cells;
+};
+
+template <typename T, int DIM, int NS>
+__device__ __forceinline__ TileGeom<DIM> tile_of(const PointLayout<T> &L, int b) {
+  TileGeom<DIM> g;
+  int bc[3] = {0, 0, 0};
+  bc[0] = b % L.nbin[0];
+  if (DIM > 1) bc[1] = (b / L.nbin[0]) % L.nbin[1];
+  if (DIM > 2) bc[2] = b / (L.nbin[0] * L.nbin[1]);
+  g.cells = 1;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (d < DIM) {
+      g.t[d] = L.bin[d] + NS;
+      g.org[d] = bc[d] * L.bin[d] - NS / 2;
+    } else {
+      g.t[d] = 1;
+      g.org[d] = 0;
+    }
+    g.cells *= g.t[d];
+  }
+  return g;
+}
+
+// x pitch of the shared tile: in 3D a multiple of 16 plus 8 words, so the four
+// rows an 8 x 4 lane patch touches start in disjoint bank octets.
+__host__ __device__ constexpr int tile_pitch_x(int dim, int tx) {
+  return dim == 3 ? (tx <= 8 ? 8 : 16 * ((tx - 8 + 15) / 16) + 8) : tx;
+}
+
+// periodic wrap of a global index that may be slightly outside [0, n)
+__device__ __forceinline__ int wrap_idx(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+// first support cell (tile coordinates) and kernel weights of one point
+template <typename T, int NS>
+__device__ __forceinline__ int point_weights(T l, int binsz, const KernelShape<T> &K, T *ker) {
+  const T sd = ceil(l - T(NS) * T(0.5));
+  int s = (int)sd + NS / 2;
+  s = s < 0 ? 0 : (s > binsz ? binsz : s);
+  eval_kernel<T, NS>(ker, sd - l, K);
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Method 2: tiled spreading in shared memory. The tile is planar (all real
+// parts, then all imaginary parts) so that consecutive cells sit in
+// consecutive banks. 3D uses one warp per point: lanes cover an 8 x 4 (x, y)
+// patch of the point's support, so the 32 atomics of one instruction hit 32
+// distinct banks (row pitch = 8 mod 32). 1D and 2D use one thread per point.
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(256)
+    spread_tile_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
+                       const cplx<T> *__restrict__ pre, int conj_pre,
+                       cplx<T> *__restrict__ fw, int64_t nf_total) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int sub = blockIdx.x;
+  const int tr = blockIdx.y;
+  const int b = L.sub_bin[sub];
+  const int p0 = L.sub_start[sub];
+  const int np = L.sub_count[sub];
+  const TileGeom<DIM> G = tile_of<T, DIM, NS>(L, b);
+  // padded pitches (3D: x pitch = 8 mod 32 words so 4 rows hit disjoint bank octets)
+  const int px = tile_pitch_x(DIM, G.t[0]);
+  const int py = G.t[1];
+  const int ncell_pad = px * py * G.t[2];
+  T *re = reinterpret_cast<T *>(smem_raw);
+  T *im = re + ncell_pad;
+  for (int i = threadIdx.x; i < ncell_pad; i += blockDim.x) {
+    re[i] = T(0);
+    im[i] = T(0);
+  }
+  __syncthreads();
+  const cplx<T> *ct = c + (int64_t)tr * L.M;
+  if constexpr (DIM < 3) {
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+      const int p = p0 + i;
+      const int j = L.perm[p];
+      cplx<T> v = ct[j];
+      if (pre) v = cmul_opt<T>(v, pre[j], conj_pre);
+      T kx[NS], ky[NS];
+      const int sx = point_weights<T, NS>(L.loc[0][p], L.bin[0], K, kx);
+      if constexpr (DIM == 1) {
+#pragma unroll
+        for (int a = 0; a < NS; ++a) {
+          atomicAdd(re + sx + a, v.x * kx[a]);
+          atomicAdd(im + sx + a, v.y * kx[a]);
+        }
+      } else {
+        const int sy = point_weights<T, NS>(L.loc[1][p], L.bin[1], K, ky);
+#pragma unroll
+        for (int bb = 0; bb < NS; ++bb) {
+          const T wr = v.x * ky[bb], wi = v.y * ky[bb];
+          const int row = (sy + bb) * px + sx;
+#pragma unroll
+          for (int a = 0; a < NS; ++a) {
+            atomicAdd(re + row + a, wr * kx[a]);
+            atomicAdd(im + row + a, wi * kx[a]);
+          }
+        }
+      }
+    }
+  } else {
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarp = blockDim.x >> 5;
+    const int lx = lane & 7;  // x offset in the support
+    const int ly = lane >> 3; // y offset within a group of 4 rows
+    for (int i = warp; i < np; i += nwarp) {
+      const int p = p0 + i;
+      const int j = L.perm[p];
+      cplx<T> v = ct[j];
+      if (pre) v = cmul_opt<T>(v, pre[j], conj_pre);
+      T kx[NS], ky[NS], kz[NS];
+      const int sx = point_weights<T, NS>(L.loc[0][p], L.bin[0], K, kx);
+      const int sy = point_weights<T, NS>(L.loc[1][p], L.bin[1], K, ky);
+      const int sz = point_weights<T, NS>(L.loc[2][p], L.bin[2], K, kz);
+      // this lane's x weight (lanes with lx >= NS idle)
+      T wx = T(0);
+#pragma unroll
+      for (int a = 0; a < NS; ++a)
+        if (a == lx) wx = kx[a];
+#pragma unroll
+      for (int yb = 0; yb < (NS + 3) / 4; ++yb) {
+        const int yy = yb * 4 + ly;
+        T wy = T(0);
+#pragma unroll
+        for (int a = 0; a < NS; ++a)
+          if (a == yy) wy = ky[a];
+        const bool on = (lx < NS) && (yy < NS);
+        const T wxy = wx * wy;
+        const int base = (sy + yy) * px + sx + lx;
+#pragma unroll
+        for (int zz = 0; zz < NS; ++zz) {
+          if (on) {
+            const T w = wxy * kz[zz];
+            const int q = base + (sz + zz) * (px * py);
+            atomicAdd(re + q, v.x * w);
+            atomicAdd(im + q, v.y * w);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // write the tile back: every tile cell adds into its periodic image
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  for (int q = threadIdx.x; q < G.cells; q += blockDim.x) {
+    const int x = q % G.t[0];
+    const int y = (q / G.t[0]) % G.t[1];
+    const int z = q / (G.t[0] * G.t[1]);
+    const int sidx = (z * py + y) * px + x;
+    cplx<T> v;
+    v.x = re[sidx];
+    v.y = im[sidx];
+    int64_t g = wrap_idx(G.org[0] + x, L.nf[0]);
+    if (DIM > 1) g += (int64_t)L.nf[0] * wrap_idx(G.org[1] + y, L.nf[1]);
+    if (DIM > 2) g += (int64_t)L.nf[0] * L.nf[1] * wrap_idx(G.org[2] + z, L.nf[2]);
+    atomic_add_cplx_global(fwt + g, v);
+  }
+}
+
+// Method 1: point-driven spreading straight into global memory with vector
+// atomics (no tile). Points are still processed in bin order for locality.
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(256)
+    spread_global_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
+                         const cplx<T> *__restrict__ pre, int conj_pre,
+                         cplx<T> *__restrict__ fw, int64_t nf_total) {
+  const int sub = blockIdx.x;
+  const int tr = blockIdx.y;
+  const int b = L.sub_bin[sub];
+  const int p0 = L.sub_start[sub];
+  const int np = L.sub_count[sub];
+  const TileGeom<DIM> G = tile_of<T, DIM, NS>(L, b);
+  const cplx<T> *ct = c + (int64_t)tr * L.M;
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    const int p = p0 + i;
+    const int j = L.perm[p];
+    cplx<T> v = ct[j];
+    if (pre) v = cmul_opt<T>(v, pre[j], conj_pre);
+    T ker[DIM][NS];
+    int gi[DIM][NS];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const int s = point_weights<T, NS>(L.loc[d][p], L.bin[d], K, ker[d]);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) gi[d][a] = wrap_idx(G.org[d] + s + a, L.nf[d]);
+    }
+    if constexpr (DIM == 1) {
+#pragma unroll
+      for (int a = 0; a < NS; ++a) {
+        cplx<T> u;
+        u.x = v.x * ker[0][a];
+        u.y = v.y * ker[0][a];
+        atomic_add_cplx_global(fwt + gi[0][a], u);
+      }
+    } else if constexpr (DIM == 2) {
+#pragma unroll
+      for (int bb = 0; bb < NS; ++bb) {
+        const int64_t row = (int64_t)gi[DIM > 1 ? 1 : 0][bb] * L.nf[0];
+        const T wr = v.x * ker[DIM > 1 ? 1 : 0][bb], wi = v.y * ker[DIM > 1 ? 1 : 0][bb];
+#pragma unroll
+        for (int a = 0; a < NS; ++a) {
+          cplx<T> u;
+          u.x = wr * ker[0][a];
+          u.y = wi * ker[0][a];
+          atomic_add_cplx_global(fwt + row + gi[0][a], u);
+        }
+      }
+    } else {
+#pragma unroll 1
+      for (int cc = 0; cc < NS; ++cc) {
+        const int64_t plane = (int64_t)gi[DIM > 2 ? 2 : 0][cc] * L.nf[0] * L.nf[1];
+        const T zr = v.x * ker[DIM > 2 ? 2 : 0][cc], zi = v.y * ker[DIM > 2 ? 2 : 0][cc];
+#pragma unroll
+        for (int bb = 0; bb < NS; ++bb) {
+          const int64_t row = plane + (int64_t)gi[DIM > 1 ? 1 : 0][bb] * L.nf[0];
+          const T wr = zr * ker[DIM > 1 ? 1 : 0][bb], wi = zi * ker[DIM > 1 ? 1 : 0][bb];
+#pragma unroll
+          for (int a = 0; a < NS; ++a) {
+            cplx<T> u;
+            u.x = wr * ker[0][a];
+            u.y = wi * ker[0][a];
+            atomic_add_cplx_global(fwt + row + gi[0][a], u);
+          }
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Interpolation: one thread per point, gathering the NS^DIM support values of
+// the fine grid (read through L1/L2: the points of a subproblem share a tile).
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(256)
+    interp_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ fw,
+                  int64_t nf_total, const cplx<T> *__restrict__ post, int conj_post,
+                  cplx<T> *__restrict__ out) {
+  const int sub = blockIdx.x;
+  const int tr = blockIdx.y;
+  const int b = L.sub_bin[sub];
+  const int p0 = L.sub_start[sub];
+  const int np = L.sub_count[sub];
+  const TileGeom<DIM> G = tile_of<T, DIM, NS>(L, b);
+  const cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  cplx<T> *ot = out + (int64_t)tr * L.M;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    const int p = p0 + i;
+    const int j = L.perm[p];
+    T ker[DIM][NS];
+    int gi[DIM][NS];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const int s = point_weights<T, NS>(L.loc[d][p], L.bin[d], K, ker[d]);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) gi[d][a] = wrap_idx(G.org[d] + s + a, L.nf[d]);
+    }
+    T accr = T(0), acci = T(0);
+    if constexpr (DIM == 1) {
+#pragma unroll
+      for (int a = 0; a < NS; ++a) {
+        const cplx<T> g = __ldg(fwt + gi[0][a]);
+        accr = fma(g.x, ker[0][a], accr);
+        acci = fma(g.y, ker[0][a], acci);
+      }
+    } else if constexpr (DIM == 2) {
+#pragma unroll
+      for (int bb = 0; bb < NS; ++bb) {
+        const int64_t row = (int64_t)gi[DIM > 1 ? 1 : 0][bb] * L.nf[0];
+        T rr = T(0), ri = T(0);
+#pragma unroll
+        for (int a = 0; a < NS; ++a) {
+          const cplx<T> g = __ldg(fwt + row + gi[0][a]);
+          rr = fma(g.x, ker[0][a], rr);
+          ri = fma(g.y, ker[0][a], ri);
+        }
+        accr = fma(rr, ker[DIM > 1 ? 1 : 0][bb], accr);
+        acci = fma(ri, ker[DIM > 1 ? 1 : 0][bb], acci);
+      }
+    } else {
+#pragma unroll 1
+      for (int cc = 0; cc < NS; ++cc) {
+        const int64_t plane = (int64_t)gi[DIM > 2 ? 2 : 0][cc] * L.nf[0] * L.nf[1];
+        T pr = T(0), pi = T(0);
+#pragma unroll
+        for (int bb = 0; bb < NS; ++bb) {
+          const int64_t row = plane + (int64_t)gi[DIM > 1 ? 1 : 0][bb] * L.nf[0];
+          T rr = T(0), ri = T(0);
+#pragma unroll
+          for (int a = 0; a < NS; ++a) {
+            const cplx<T> g = __ldg(fwt + row + gi[0][a]);
+            rr = fma(g.x, ker[0][a], rr);
+            ri = fma(g.y, ker[0][a], ri);
+          }
+          pr = fma(rr, ker[DIM > 1 ? 1 : 0][bb], pr);
+          pi = fma(ri, ker[DIM > 1 ? 1 : 0][bb], pi);
+        }
+        accr = fma(pr, ker[DIM > 2 ? 2 : 0][cc], accr);
+        acci = fma(pi, ker[DIM > 2 ? 2 : 0][cc], acci);
+      }
+    }
+    cplx<T> r;
+    r.x = accr;
+    r.y = acci;
+    if (post) r = cmul_opt<T>(r, post[j], conj_post);
+    ot[j] = r;
+  }
+}
+
+// ------------------------------------------------------------- dispatch ----
+template <typename T, int DIM> struct Dispatch {
+  template <int NS>
+  static void spread(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *c,
+                     const cplx<T> *pre, int conj_pre, cplx<T> *fw, int64_t nf_total, int ntr,
+                     const SpreadConfig &cfg, cudaStream_t s) {
+    dim3 grid((unsigned)L.nsub, (unsigned)ntr);
+    if (cfg.method == 1) {
+      spread_global_kernel<T, DIM, NS><<<grid, cfg.threads, 0, s>>>(L, K, c, pre, conj_pre, fw,
+                                                                    nf_total);
+    } else {
+      auto kern = spread_tile_kernel<T, DIM, NS>;
+      GBN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)cfg.smem));
+      kern<<<grid, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
+    }
+    GBN_LAUNCH_CHECK();
+  }
+  template <int NS>
+  static void interp(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *fw,
+                     int64_t nf_total, const cplx<T> *post, int conj_post, cplx<T> *out,
+                     int ntr, cudaStream_t s) {
+    dim3 grid((unsigned)L.nsub, (unsigned)ntr);
+    interp_kernel<T, DIM, NS><<<grid, 128, 0, s>>>(L, K, fw, nf_total, post, conj_post, out);
+    GBN_LAUNCH_CHECK();
+  }
+};
+
+template <typename T, int DIM, typename F> void ns_switch(int ns, F &&f) {
+  switch (ns) {
+  case 2: f.template operator()<2>(); break;
+  case 3: f.template operator()<3>(); break;
+  case 4: f.template operator()<4>(); break;
+  case 5: f.template operator()<5>(); break;
+  case 6: f.template operator()<6>(); break;
+  case 7: f.template operator()<7>(); break;
+  case 8: f.template operator()<8>(); break;
+  case 9: f.template operator()<9>(); break;
+  case 10: f.template operator()<10>(); break;
+  case 11: f.template operator()<11>(); break;
+  case 12: f.template operator()<12>(); break;
+  default:
+    if constexpr (std::is_same_v<T, double>) {
+      switch (ns) {
+      case 13: f.template operator()<13>(); break;
+      case 14: f.template operator()<14>(); break;
+      case 15: f.template operator()<15>(); break;
+      case 16: f.template operator()<16>(); break;
+      default: GBN_THROW(FINUFFT_ERR_SPREAD_BOX_SMALL, "unsupported kernel width");
+      }
+    } else {
+      GBN_THROW(FINUFFT_ERR_SPREAD_BOX_SMALL, "unsupported kernel width");
+    }
+  }
+}
+
+template <typename T, int DIM>
+void spread_dim(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *c,
+                const cplx<T> *pre, int conj_pre, cplx<T> *fw, int64_t nf_total, int ntr,
+                const SpreadConfig &cfg, cudaStream_t s) {
+  ns_switch<T, DIM>(K.ns, [&]<int NS>() {
+    Dispatch<T, DIM>::template spread<NS>(L, K, c, pre, conj_pre, fw, nf_total, ntr, cfg, s);
+  });
+}
+
+template <typename T, int DIM>
+void interp_dim(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *fw,
+                int64_t nf_total, const cplx<T> *post, int conj_post, cplx<T> *out, int ntr,
+                cudaStream_t s) {
+  ns_switch<T, DIM>(K.ns, [&]<int NS>() {
+    Dispatch<T, DIM>::template interp<NS>(L, K, fw, nf_total, post, conj_post, out, ntr, s);
+  });
+}
+
+} // namespace gbn

@@ -1,0 +1,61 @@
+/* Extensions of the GB300 NUFFT engine. None of these has a counterpart in
+ * the reference C API; existing cufinufft/finufft callers never need them.
+ * They expose the adjoint on device pointers, plan introspection, per-stage
+ * timing and CUDA-graph replay of execute.
+ */
+#ifndef GBNUFFT_EXT_H
+#define GBNUFFT_EXT_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "cufinufft.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbnufft_plan_info {
+  int type, dim, ntransf, batchsize;
+  int ns;              /* kernel width */
+  double beta;         /* ES kernel shape */
+  double upsampfac;    /* sigma actually used */
+  int nf[3];           /* fine grid (type 3: outer grid) */
+  int bins[3];         /* bin size per dimension */
+  int method;          /* 1 global atomics, 2 shared-memory tiles */
+  int nsub;            /* subproblems after setpts */
+  int64_t M, N;        /* points / targets after setpts */
+  size_t spread_smem;  /* shared memory per spread block (method 2) */
+  double horner_err;   /* max abs error of the fitted kernel pieces */
+  int inner_nf[3];     /* type 3: fine grid of the inner type-2 plan */
+} gbnufft_plan_info;
+
+#define GBNUFFT_EXT_DECLS(P, PLAN, T, C)                                                   \
+  /* Adjoint of the planned transform on device pointers (type 1 and 3: fk in,      */  \
+  /* c out; type 2: c in, fk out), same semantics as finufft_execute_adjoint.       */  \
+  GBNUFFT_EXPORT int P##_execute_adjoint(PLAN plan, C *d_c, C *d_fk);                    \
+  GBNUFFT_EXPORT int P##_plan_info(PLAN plan, gbnufft_plan_info *info);                  \
+  /* enable != 0 turns on CUDA-event timing of the stages of later executes;        */  \
+  /* ms[0..3] = spread-or-interp, FFT, deconvolve-or-amplify, total of the last one */  \
+  GBNUFFT_EXPORT int P##_stage_times(PLAN plan, int enable, float ms[4]);                \
+  /* Copies the device bin sort to host arrays: perm[M] (sorted position -> input   */  \
+  /* index) and loc[dim*M] (bin-local coordinates, dimension-major).                */  \
+  GBNUFFT_EXPORT int P##_get_sort(PLAN plan, int *perm, T *loc);                         \
+  /* Captures execute(d_c, d_fk) into a CUDA graph on the plan's stream (which must */  \
+  /* not be the legacy default stream); graph_launch replays it on that stream.     */  \
+  GBNUFFT_EXPORT int P##_graph_capture(PLAN plan, C *d_c, C *d_fk);                      \
+  GBNUFFT_EXPORT int P##_graph_launch(PLAN plan);
+
+GBNUFFT_EXT_DECLS(cufinufft, cufinufft_plan, double, cuDoubleComplex)
+GBNUFFT_EXT_DECLS(cufinufftf, cufinufftf_plan, float, cuFloatComplex)
+
+/* Measures the device's conflict-free shared-memory f32 atomicAdd rate
+ * (lane operations per second), the peak the spreading kernels are held to. */
+GBNUFFT_EXPORT int gbnufft_smem_atomic_rate(int device, double *rate);
+
+/* Library build identification string. */
+GBNUFFT_EXPORT const char *gbnufft_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

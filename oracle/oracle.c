@@ -1,0 +1,545 @@
+/* oracle.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of flatironinstitute/finufft arithmetic, used by tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker.
+ * Nothing in the GB300 engine links, loads or calls this file.
+ *
+ * Contents (each function cites the reference code it follows):
+ *   - FP64 direct NUDFTs of types 1, 2, 3 in 1D/2D/3D (test/utils/dirft1d.hpp,
+ *     dirft2d.hpp, dirft3d.hpp), on all or a sampled subset of outputs;
+ *   - planning math: next235, Gauss-Legendre nodes, GPU kernel width/beta,
+ *     type-3 grid (src/common/utils.cpp, src/cuda/makeplan.cu:43-119,
+ *     include/finufft_common/kernel.h:165-181);
+ *   - the engine's FP64 fold-rescale and a stable counting sort by bin,
+ *     the host replica the device permutation must match bit for bit;
+ *   - spreading / interpolation with the ES kernel in FP64 (the GPU library's
+ *     kernel, include/cufinufft/spreadinterp.hpp:29-39);
+ *   - an OpenMP subproblem spreader/interpolator with a tabulated
+ *     piecewise-polynomial kernel (the CPU library's design,
+ *     include/finufft/spreadinterp.hpp:310-485, spread.hpp:53-451) used for
+ *     the CPU FINUFFT restatement with its PSWF kernel.
+ * Complex arrays are interleaved (re, im) doubles or floats.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define OR_PI 3.141592653589793238462643383279502884
+#define OR_INV_2PI 0.159154943091895335768883763372514362
+
+/* ------------------------------------------------------------ planning ---- */
+
+static int smooth235(int64_t n) {
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  while (n % 5 == 0) n /= 5;
+  return n == 1;
+}
+
+/* next235(n, 2) of src/common/utils.cpp:117-121: 2*(smallest smooth m, 2m >= n) */
+int64_t or_next235_even(int64_t n) {
+  if (n < 1) n = 1;
+  int64_t m = (n + 1) / 2;
+  while (!smooth235(m)) ++m;
+  return 2 * m;
+}
+
+/* n-node Gauss-Legendre nodes (ascending) and weights via Newton on the
+ * three-term Legendre recurrence (src/common/utils.cpp:17-57). */
+void or_gauss_legendre(int n, double *x, double *w) {
+  for (int i = 0; i < (n + 1) / 2; ++i) {
+    double z = cos(OR_PI * (i + 0.75) / (n + 0.5)), p0 = 1, p1 = z, dp = 1;
+    for (int it = 0; it < 100; ++it) {
+      p0 = 1.0;
+      p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-16) break;
+    }
+    p0 = 1.0;
+    p1 = z;
+    for (int k = 2; k <= n; ++k) {
+      double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = (n == 1) ? 1.0 : n * (z * p1 - p0) / (z * z - 1.0);
+    x[i] = -z;
+    x[n - 1 - i] = z;
+    w[i] = w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+  if (n % 2 == 1) x[n / 2] = 0.0;
+}
+
+/* GPU kernel width and beta (src/cuda/makeplan.cu:43-119), arithmetic in the
+ * plan precision (is_float). Returns ns; beta in *beta. Error codes as the
+ * reference: -8 Horner with nonstandard sigma, -7 sigma <= 1. */
+int or_gpu_kernel(double tol, double sigma, int kerevalmeth, int is_float, double *beta) {
+  if (sigma != 2.0 && sigma != 1.25) {
+    if (kerevalmeth == 1) return -8;
+    if (sigma <= 1.0) return -7;
+  }
+  int ns;
+  if (is_float) {
+    float eps = (float)tol, s = (float)sigma;
+    if (eps < 1.1920929e-7f) eps = 1.1920929e-7f;
+    ns = (int)ceilf(-log10f(eps / 10.0f));
+    if (s != 2.0f) ns = (int)ceilf(-logf(eps) / ((float)OR_PI * sqrtf(1.0f - 1.0f / s)));
+    if (ns < 2) ns = 2;
+    if (ns > 12) ns = 12;
+    float bon = 2.30f;
+    if (ns == 2) bon = 2.20f;
+    if (ns == 3) bon = 2.26f;
+    if (ns == 4) bon = 2.38f;
+    if (s != 2.0f) bon = 0.97f * (float)OR_PI * (1.0f - 1.0f / (2.0f * s));
+    *beta = (double)(bon * (float)ns);
+  } else {
+    double eps = tol;
+    if (eps < 2.220446049250313e-16) eps = 2.220446049250313e-16;
+    ns = (int)ceil(-log10(eps / 10.0));
+    if (sigma != 2.0) ns = (int)ceil(-log(eps) / (OR_PI * sqrt(1.0 - 1.0 / sigma)));
+    if (ns < 2) ns = 2;
+    if (ns > 16) ns = 16;
+    double bon = 2.30;
+    if (ns == 2) bon = 2.20;
+    if (ns == 3) bon = 2.26;
+    if (ns == 4) bon = 2.38;
+    if (sigma != 2.0) bon = 0.97 * OR_PI * (1.0 - 1.0 / (2.0 * sigma));
+    *beta = bon * ns;
+  }
+  return ns;
+}
+
+/* type 1/2 fine grid (src/cuda/fft.cu:166-179) */
+int64_t or_fine_grid(int64_t ms, double sigma, int ns) {
+  int64_t nf = (int64_t)ceil(sigma * (double)ms);
+  if (nf < 2 * ns) nf = 2 * ns;
+  if (nf < 2147483647LL) nf = or_next235_even(nf);
+  return nf;
+}
+
+/* type-3 grid (include/finufft_common/kernel.h:165-181): out = {nf, h, gam} */
+void or_type3_grid(double sigma, double X, double S, int ns, double *out) {
+  double Xs = X, Ss = S;
+  if (Xs == 0.0) {
+    if (Ss == 0.0) Xs = Ss = 1.0;
+    else Xs = 1.0 / Ss;
+  } else if (Ss < 1.0 / Xs)
+    Ss = 1.0 / Xs;
+  double nfd = 2.0 * sigma * Ss * Xs / OR_PI + (ns + 1);
+  if (!isfinite(nfd)) nfd = 0.0;
+  int64_t nf = (int64_t)nfd;
+  if (nf < 2 * ns) nf = 2 * ns;
+  if (nf < 2147483647LL) nf = or_next235_even(nf);
+  out[0] = (double)nf;
+  out[1] = 2.0 * OR_PI / (double)nf;
+  out[2] = (double)nf / (2.0 * sigma * Ss);
+}
+
+double or_es_kernel(double x, int ns, double beta) {
+  double z = 2.0 * x / ns;
+  if (fabs(z) >= 1.0) return 0.0;
+  return exp(beta * (sqrt(1.0 - z * z) - 1.0));
+}
+
+/* --------------------------------------------------- fold and bin sort ---- */
+
+/* The engine's fold: y = (x - shift)*scale, r = frac(y/2pi + 1/2)*nf in FP64
+ * with round-to-nearest steps (compile with -ffp-contract=off), NaN -> 0,
+ * cell = floor(r) wrapped, frac = r - floor(r). */
+void or_fold_cell(double x, double shift, double scale, int nf, int *cell, double *frac) {
+  double y = (x - shift) * scale;
+  double r = fma(y, OR_INV_2PI, 0.5);
+  r = r - floor(r);
+  r = r * (double)nf;
+  if (!(r >= 0.0 && r <= (double)nf)) r = 0.0;
+  double fl = floor(r);
+  int c = (int)fl;
+  if (c >= nf) c -= nf;
+  *cell = c;
+  *frac = r - fl;
+}
+
+/* Stable counting sort by bin (x fastest), as the CPU library's bin sort
+ * (include/finufft/spread.hpp:459-584) but with the engine's fold and integer
+ * bins. coords: dim arrays of doubles (the caller converts float inputs
+ * exactly). Outputs perm[M] and loc[dim*M] (bin-local coordinates, rounded to
+ * float when loc_is_float). Returns 0. */
+int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *shift,
+                const double *scale, const int *nf, const int *bin, int32_t *perm,
+                void *loc, int loc_is_float) {
+  int nb[3] = {1, 1, 1};
+  for (int d = 0; d < dim; ++d) nb[d] = (nf[d] + bin[d] - 1) / bin[d];
+  int64_t nbins = (int64_t)nb[0] * nb[1] * nb[2];
+  int64_t *cnt = (int64_t *)calloc((size_t)nbins + 1, sizeof(int64_t));
+  uint32_t *key = (uint32_t *)malloc((size_t)(M > 0 ? M : 1) * sizeof(uint32_t));
+  for (int64_t i = 0; i < M; ++i) {
+    uint32_t k = 0, stride = 1;
+    for (int d = 0; d < dim; ++d) {
+      int c;
+      double f;
+      or_fold_cell(coords[d][i], shift[d], scale[d], nf[d], &c, &f);
+      k += stride * (uint32_t)(c / bin[d]);
+      stride *= (uint32_t)nb[d];
+    }
+    key[i] = k;
+    cnt[k + 1]++;
+  }
+  for (int64_t b = 0; b < nbins; ++b) cnt[b + 1] += cnt[b];
+  for (int64_t i = 0; i < M; ++i) perm[cnt[key[i]]++] = (int32_t)i;
+  for (int64_t p = 0; p < M; ++p) {
+    int64_t i = perm[p];
+    for (int d = 0; d < dim; ++d) {
+      int c;
+      double f;
+      or_fold_cell(coords[d][i], shift[d], scale[d], nf[d], &c, &f);
+      double l = (double)(c - (c / bin[d]) * bin[d]) + f;
+      if (loc_is_float) ((float *)loc)[(size_t)d * M + p] = (float)l;
+      else ((double *)loc)[(size_t)d * M + p] = l;
+    }
+  }
+  free(cnt);
+  free(key);
+  return 0;
+}
+
+/* ------------------------------------------------------- direct sums ---- */
+
+/* mode index of CMCL-ordered position i along an axis of length n */
+static inline int64_t or_mode(int64_t i, int64_t n) { return i - n / 2; }
+
+/* Type 1 (test/utils/dirft*d.hpp): f[k] = sum_j c[j] exp(i isign k.x_j) at the
+ * modes with flat CMCL positions kidx[0..nk) (x fastest); kidx NULL = all modes. */
+void or_dirft1(int dim, int64_t M, const double *const *xyz, const double *c, int isign,
+               const int64_t *nm, int64_t nk, const int64_t *kidx, double *out) {
+  const double sg = isign >= 0 ? 1.0 : -1.0;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t q = 0; q < nk; ++q) {
+    int64_t flat = kidx ? kidx[q] : q;
+    double k[3] = {0, 0, 0};
+    k[0] = (double)or_mode(flat % nm[0], nm[0]);
+    if (dim > 1) k[1] = (double)or_mode((flat / nm[0]) % nm[1], nm[1]);
+    if (dim > 2) k[2] = (double)or_mode(flat / (nm[0] * nm[1]), nm[2]);
+    double sr = 0, si = 0;
+    for (int64_t j = 0; j < M; ++j) {
+      double ph = k[0] * xyz[0][j];
+      if (dim > 1) ph += k[1] * xyz[1][j];
+      if (dim > 2) ph += k[2] * xyz[2][j];
+      double cs = cos(ph), sn = sg * sin(ph);
+      sr += c[2 * j] * cs - c[2 * j + 1] * sn;
+      si += c[2 * j] * sn + c[2 * j + 1] * cs;
+    }
+    out[2 * q] = sr;
+    out[2 * q + 1] = si;
+  }
+}
+
+/* Type 2: c[j] = sum_k f[k] exp(i isign k.x_j) for the points jidx[0..nj)
+ * (NULL = all M); f has all modes in CMCL order. */
+void or_dirft2(int dim, int64_t M, const double *const *xyz, int isign, const int64_t *nm,
+               const double *f, int64_t nj, const int64_t *jidx, double *out) {
+  const double sg = isign >= 0 ? 1.0 : -1.0;
+  const int64_t ntot = nm[0] * (dim > 1 ? nm[1] : 1) * (dim > 2 ? nm[2] : 1);
+  (void)M;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t q = 0; q < nj; ++q) {
+    int64_t j = jidx ? jidx[q] : q;
+    double sr = 0, si = 0;
+    for (int64_t flat = 0; flat < ntot; ++flat) {
+      double ph = (double)or_mode(flat % nm[0], nm[0]) * xyz[0][j];
+      if (dim > 1) ph += (double)or_mode((flat / nm[0]) % nm[1], nm[1]) * xyz[1][j];
+      if (dim > 2) ph += (double)or_mode(flat / (nm[0] * nm[1]), nm[2]) * xyz[2][j];
+      double cs = cos(ph), sn = sg * sin(ph);
+      sr += f[2 * flat] * cs - f[2 * flat + 1] * sn;
+      si += f[2 * flat] * sn + f[2 * flat + 1] * cs;
+    }
+    out[2 * q] = sr;
+    out[2 * q + 1] = si;
+  }
+}
+
+/* Type 3: f[k] = sum_j c[j] exp(i isign s_k.x_j) for targets kidx[0..nk) (NULL = all). */
+void or_dirft3(int dim, int64_t M, const double *const *xyz, const double *c, int isign,
+               const double *const *stu, int64_t nk, const int64_t *kidx, double *out) {
+  const double sg = isign >= 0 ? 1.0 : -1.0;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t q = 0; q < nk; ++q) {
+    int64_t k = kidx ? kidx[q] : q;
+    double sr = 0, si = 0;
+    for (int64_t j = 0; j < M; ++j) {
+      double ph = stu[0][k] * xyz[0][j];
+      if (dim > 1) ph += stu[1][k] * xyz[1][j];
+      if (dim > 2) ph += stu[2][k] * xyz[2][j];
+      double cs = cos(ph), sn = sg * sin(ph);
+      sr += c[2 * j] * cs - c[2 * j + 1] * sn;
+      si += c[2 * j] * sn + c[2 * j + 1] * cs;
+    }
+    out[2 * q] = sr;
+    out[2 * q + 1] = si;
+  }
+}
+
+/* ------------------------------------------- ES spread / interp (FP64) ---- */
+
+/* Grid weights of one point along one axis with the ES kernel: first cell
+ * (wrapped into [0,nf)) and ns kernel values, as the GPU library places a point
+ * (include/cufinufft/spreadinterp.hpp:166-196) but from the engine's FP64 fold. */
+static void or_axis_es(double x, double shift, double scale, int nf, int ns, double beta,
+                       int *start, double *ker) {
+  int c;
+  double f;
+  or_fold_cell(x, shift, scale, nf, &c, &f);
+  double r = (double)c + f;
+  double s = ceil(r - 0.5 * ns);
+  for (int j = 0; j < ns; ++j) ker[j] = or_es_kernel(s - r + j, ns, beta);
+  int st = (int)s % nf;
+  if (st < 0) st += nf;
+  *start = st;
+}
+
+/* grid[g] += sum_j c_j phi(g - r_j) over the periodic grid nf[0..dim) (x fastest). */
+void or_spread_es(int dim, int64_t M, const double *const *xyz, const double *shift,
+                  const double *scale, const double *c, const int *nf, int ns, double beta,
+                  double *grid) {
+  double ker[3][32];
+  int st[3] = {0, 0, 0};
+  const int n1 = dim > 1 ? ns : 1, n2 = dim > 2 ? ns : 1;
+  for (int64_t j = 0; j < M; ++j) {
+    for (int d = 0; d < dim; ++d)
+      or_axis_es(xyz[d][j], shift[d], scale[d], nf[d], ns, beta, &st[d], ker[d]);
+    for (int cz = 0; cz < n2; ++cz) {
+      int64_t gz = dim > 2 ? (st[2] + cz) % nf[2] : 0;
+      double wz = dim > 2 ? ker[2][cz] : 1.0;
+      for (int cy = 0; cy < n1; ++cy) {
+        int64_t gy = dim > 1 ? (st[1] + cy) % nf[1] : 0;
+        double wy = wz * (dim > 1 ? ker[1][cy] : 1.0);
+        for (int cx = 0; cx < ns; ++cx) {
+          int64_t gx = (st[0] + cx) % nf[0];
+          int64_t g = gx + (int64_t)nf[0] * (gy + (int64_t)(dim > 1 ? nf[1] : 1) * gz);
+          double w = wy * ker[0][cx];
+          grid[2 * g] += w * c[2 * j];
+          grid[2 * g + 1] += w * c[2 * j + 1];
+        }
+      }
+    }
+  }
+}
+
+/* c[j] = sum_g grid[g] phi(g - r_j) */
+void or_interp_es(int dim, int64_t M, const double *const *xyz, const double *shift,
+                  const double *scale, const double *grid, const int *nf, int ns, double beta,
+                  double *c) {
+  const int n1 = dim > 1 ? ns : 1, n2 = dim > 2 ? ns : 1;
+#pragma omp parallel for schedule(static)
+  for (int64_t j = 0; j < M; ++j) {
+    double ker[3][32];
+    int st[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d)
+      or_axis_es(xyz[d][j], shift[d], scale[d], nf[d], ns, beta, &st[d], ker[d]);
+    double sr = 0, si = 0;
+    for (int cz = 0; cz < n2; ++cz) {
+      int64_t gz = dim > 2 ? (st[2] + cz) % nf[2] : 0;
+      double wz = dim > 2 ? ker[2][cz] : 1.0;
+      for (int cy = 0; cy < n1; ++cy) {
+        int64_t gy = dim > 1 ? (st[1] + cy) % nf[1] : 0;
+        double wy = wz * (dim > 1 ? ker[1][cy] : 1.0);
+        for (int cx = 0; cx < ns; ++cx) {
+          int64_t gx = (st[0] + cx) % nf[0];
+          int64_t g = gx + (int64_t)nf[0] * (gy + (int64_t)(dim > 1 ? nf[1] : 1) * gz);
+          double w = wy * ker[0][cx];
+          sr += w * grid[2 * g];
+          si += w * grid[2 * g + 1];
+        }
+      }
+    }
+    c[2 * j] = sr;
+    c[2 * j + 1] = si;
+  }
+}
+
+/* ------------------------- CPU-library-style spreader (OpenMP, Horner) ---- */
+/* The CPU library spreads bin-sorted points in subproblems: each thread fills
+ * a private padded box, then adds it into the periodic fine grid
+ * (include/finufft/spreadinterp.hpp:310-485, include/finufft/spread.hpp:53-451).
+ * The kernel is given as ns pieces of ncoef Horner coefficients in
+ * u = 2(x - piece start) - 1 (coef[k*ns + j], k = 0 highest degree); for the
+ * CPU restatement they are fitted to the PSWF kernel by the Python side.
+ * Arithmetic is in the plan precision T, as in the CPU library. */
+
+#define OR_MAXNS 16
+#define OR_DEFINE_CPU(T, SUF)                                                                \
+  /* fold (include/finufft/simd.hpp:318-325) and first cell / kernel argument */            \
+  static inline void or_place_##SUF(T x, int nf, int ns, int *i1, T *t0) {                  \
+    T r = (T)fma(x, (T)OR_INV_2PI, (T)0.5);                                                  \
+    r = (r - floor(r)) * (T)nf;                                                              \
+    T s = ceil(r - (T)0.5 * ns);                                                             \
+    *i1 = (int)s;                                                                            \
+    *t0 = s - r;                                                                             \
+  }                                                                                          \
+  static inline void or_horner_##SUF(const double *coef, int ns, int nc, T t0, T *ker) {    \
+    T u = (T)2 * t0 + (T)(ns - 1);                                                           \
+    for (int j = 0; j < ns; ++j) ker[j] = (T)coef[j];                                        \
+    for (int k = 1; k < nc; ++k)                                                             \
+      for (int j = 0; j < ns; ++j) ker[j] = ker[j] * u + (T)coef[k * ns + j];               \
+  }                                                                                          \
+  /* bin-sort permutation (CPU bins 16 x 4 x 4, stable) */                                  \
+  void or_cpu_sort_##SUF(int dim, int64_t M, const T *const *xyz, const int *nf,            \
+                         int32_t *perm) {                                                    \
+    const int bs[3] = {16, 4, 4};                                                            \
+    int nb[3] = {1, 1, 1};                                                                   \
+    for (int d = 0; d < dim; ++d) nb[d] = nf[d] / bs[d] + 1;                                 \
+    int64_t nbins = (int64_t)nb[0] * nb[1] * nb[2];                                          \
+    int64_t *cnt = (int64_t *)calloc((size_t)nbins + 1, sizeof(int64_t));                    \
+    uint32_t *key = (uint32_t *)malloc((size_t)(M > 0 ? M : 1) * sizeof(uint32_t));          \
+    _Pragma("omp parallel for schedule(static)") for (int64_t i = 0; i < M; ++i) {         \
+      int64_t k = 0, st = 1;                                                                 \
+      for (int d = 0; d < dim; ++d) {                                                        \
+        T r = (T)fma(xyz[d][i], (T)OR_INV_2PI, (T)0.5);                                      \
+        r = (r - floor(r)) * (T)nf[d];                                                       \
+        int b = (int)(r / bs[d]);                                                            \
+        if (b >= nb[d]) b = nb[d] - 1;                                                       \
+        if (b < 0) b = 0;                                                                    \
+        k += st * b;                                                                         \
+        st *= nb[d];                                                                         \
+      }                                                                                      \
+      key[i] = (uint32_t)k;                                                                  \
+    }                                                                                        \
+    for (int64_t i = 0; i < M; ++i) cnt[key[i] + 1]++;                                       \
+    for (int64_t b = 0; b < nbins; ++b) cnt[b + 1] += cnt[b];                                \
+    for (int64_t i = 0; i < M; ++i) perm[cnt[key[i]]++] = (int32_t)i;                        \
+    free(cnt);                                                                               \
+    free(key);                                                                               \
+  }                                                                                          \
+  /* grid (zeroed by caller) += spread of c over sorted points, subproblems of <= maxsub */ \
+  void or_cpu_spread_##SUF(int dim, int64_t M, const T *const *xyz, const int32_t *perm,    \
+                           const T *c, const int *nf, int ns, int nc, const double *coef,   \
+                           int maxsub, T *grid) {                                            \
+    const int64_t nsub = (M + maxsub - 1) / maxsub;                                          \
+    const int64_t n0 = nf[0], n1 = dim > 1 ? nf[1] : 1, n2 = dim > 2 ? nf[2] : 1;           \
+    _Pragma("omp parallel for schedule(dynamic, 1)") for (int64_t sp = 0; sp < nsub; ++sp) { \
+      const int64_t p0 = sp * maxsub, p1 = p0 + maxsub < M ? p0 + maxsub : M;                \
+      int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-(1 << 30), -(1 << 30), -(1 << 30)}; \
+      for (int64_t p = p0; p < p1; ++p)                                                      \
+        for (int d = 0; d < dim; ++d) {                                                      \
+          int i1;                                                                            \
+          T t0;                                                                              \
+          or_place_##SUF(xyz[d][perm[p]], nf[d], ns, &i1, &t0);                              \
+          if (i1 < lo[d]) lo[d] = i1;                                                        \
+          if (i1 > hi[d]) hi[d] = i1;                                                        \
+        }                                                                                    \
+      int64_t ext[3] = {1, 1, 1};                                                            \
+      for (int d = 0; d < dim; ++d) ext[d] = hi[d] - lo[d] + ns;                             \
+      T *box = (T *)calloc((size_t)(2 * ext[0] * ext[1] * ext[2]), sizeof(T));               \
+      T kx[OR_MAXNS], ky[OR_MAXNS], kz[OR_MAXNS];                                            \
+      for (int64_t p = p0; p < p1; ++p) {                                                    \
+        const int64_t j = perm[p];                                                           \
+        int ix, iy = 0, iz = 0;                                                              \
+        T t0;                                                                                \
+        or_place_##SUF(xyz[0][j], nf[0], ns, &ix, &t0);                                      \
+        or_horner_##SUF(coef, ns, nc, t0, kx);                                               \
+        if (dim > 1) {                                                                       \
+          or_place_##SUF(xyz[1][j], nf[1], ns, &iy, &t0);                                    \
+          or_horner_##SUF(coef, ns, nc, t0, ky);                                             \
+        } else                                                                               \
+          ky[0] = 1;                                                                         \
+        if (dim > 2) {                                                                       \
+          or_place_##SUF(xyz[2][j], nf[2], ns, &iz, &t0);                                    \
+          or_horner_##SUF(coef, ns, nc, t0, kz);                                             \
+        } else                                                                               \
+          kz[0] = 1;                                                                         \
+        const T cr = c[2 * j], ci = c[2 * j + 1];                                            \
+        const int ny = dim > 1 ? ns : 1, nz = dim > 2 ? ns : 1;                              \
+        for (int a = 0; a < nz; ++a)                                                         \
+          for (int b = 0; b < ny; ++b) {                                                     \
+            const T w = ky[b] * kz[a];                                                       \
+            const T wr = cr * w, wi = ci * w;                                                \
+            T *row = box + 2 * ((ix - lo[0]) +                                               \
+                                ext[0] * ((dim > 1 ? iy - lo[1] + b : 0) +                   \
+                                          ext[1] * (dim > 2 ? iz - lo[2] + a : 0)));         \
+            for (int q = 0; q < ns; ++q) {                                                   \
+              row[2 * q] += wr * kx[q];                                                      \
+              row[2 * q + 1] += wi * kx[q];                                                  \
+            }                                                                                \
+          }                                                                                  \
+      }                                                                                      \
+      for (int64_t bz = 0; bz < ext[2]; ++bz) {                                              \
+        int64_t gz = dim > 2 ? ((lo[2] + bz) % n2 + n2) % n2 : 0;                            \
+        for (int64_t by = 0; by < ext[1]; ++by) {                                            \
+          int64_t gy = dim > 1 ? ((lo[1] + by) % n1 + n1) % n1 : 0;                          \
+          const T *row = box + 2 * ext[0] * (by + ext[1] * bz);                              \
+          for (int64_t bx = 0; bx < ext[0]; ++bx) {                                          \
+            int64_t gx = ((lo[0] + bx) % n0 + n0) % n0;                                      \
+            T *g = grid + 2 * (gx + n0 * (gy + n1 * gz));                                    \
+            _Pragma("omp atomic") g[0] += row[2 * bx];                                       \
+            _Pragma("omp atomic") g[1] += row[2 * bx + 1];                                   \
+          }                                                                                  \
+        }                                                                                    \
+      }                                                                                      \
+      free(box);                                                                             \
+    }                                                                                        \
+  }                                                                                          \
+  /* c[j] = interpolation of the periodic grid at the points (sorted traversal) */          \
+  void or_cpu_interp_##SUF(int dim, int64_t M, const T *const *xyz, const int32_t *perm,    \
+                           const T *grid, const int *nf, int ns, int nc, const double *coef, \
+                           T *c) {                                                           \
+    const int64_t n0 = nf[0], n1 = dim > 1 ? nf[1] : 1, n2 = dim > 2 ? nf[2] : 1;           \
+    _Pragma("omp parallel for schedule(static, 4096)") for (int64_t p = 0; p < M; ++p) {    \
+      const int64_t j = perm[p];                                                             \
+      T kx[OR_MAXNS], ky[OR_MAXNS], kz[OR_MAXNS];                                            \
+      int ix, iy = 0, iz = 0;                                                                \
+      T t0;                                                                                  \
+      or_place_##SUF(xyz[0][j], nf[0], ns, &ix, &t0);                                        \
+      or_horner_##SUF(coef, ns, nc, t0, kx);                                                 \
+      if (dim > 1) {                                                                         \
+        or_place_##SUF(xyz[1][j], nf[1], ns, &iy, &t0);                                      \
+        or_horner_##SUF(coef, ns, nc, t0, ky);                                               \
+      } else                                                                                 \
+        ky[0] = 1;                                                                           \
+      if (dim > 2) {                                                                         \
+        or_place_##SUF(xyz[2][j], nf[2], ns, &iz, &t0);                                      \
+        or_horner_##SUF(coef, ns, nc, t0, kz);                                               \
+      } else                                                                                 \
+        kz[0] = 1;                                                                           \
+      T sr = 0, si = 0;                                                                      \
+      const int ny = dim > 1 ? ns : 1, nz = dim > 2 ? ns : 1;                                \
+      for (int a = 0; a < nz; ++a) {                                                         \
+        int64_t gz = dim > 2 ? ((iz + a) % n2 + n2) % n2 : 0;                                \
+        for (int b = 0; b < ny; ++b) {                                                       \
+          int64_t gy = dim > 1 ? ((iy + b) % n1 + n1) % n1 : 0;                              \
+          const T w = ky[b] * kz[a];                                                         \
+          T rr = 0, ri = 0;                                                                  \
+          for (int q = 0; q < ns; ++q) {                                                     \
+            int64_t gx = ((ix + q) % n0 + n0) % n0;                                          \
+            const T *g = grid + 2 * (gx + n0 * (gy + n1 * gz));                              \
+            rr += kx[q] * g[0];                                                              \
+            ri += kx[q] * g[1];                                                              \
+          }                                                                                  \
+          sr += w * rr;                                                                      \
+          si += w * ri;                                                                      \
+        }                                                                                    \
+      }                                                                                      \
+      c[2 * j] = sr;                                                                         \
+      c[2 * j + 1] = si;                                                                     \
+    }                                                                                        \
+  }
+
+OR_DEFINE_CPU(float, f)
+OR_DEFINE_CPU(double, d)
+
+int or_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}

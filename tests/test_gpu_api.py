@@ -1,0 +1,275 @@
+"""GPU tests of the drop-in API: error codes that need the device
+(test/cuda/test_makeplan.c), many-vector batches, mode ordering,
+spread/interp-only mode, adjoints, the host-pointer finufft_* interface, the
+simple interfaces, CUDA-graph replay and edge cases."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _cx(rng, shape, dt="complex64"):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(dt)
+
+
+def _mk(engine, pfx, ty, dim, modes, ntr=1, tol=1e-5, opts=None):
+    p = ctypes.c_void_p()
+    m = (ctypes.c_int64 * 3)(*modes)
+    ier = getattr(engine, pfx + "_makeplan")(ty, dim, m, 1, ntr, tol, ctypes.byref(p),
+                                             ctypes.byref(opts) if opts else None)
+    if ier == 0:
+        getattr(engine, pfx + "_destroy")(p)
+    return ier
+
+
+def test_makeplan_error_codes(engine):
+    from finufft_gb300 import _lib
+
+    N = (10, 20, 15)
+    for dim in (1, 2, 3):
+        assert _mk(engine, "cufinufftf", 1, dim, N) == 0
+        assert _mk(engine, "cufinufftf", 4, dim, N) == 10  # FINUFFT_ERR_TYPE_NOTVALID
+        assert _mk(engine, "cufinufftf", 1, dim, N, ntr=0) == 9  # FINUFFT_ERR_NTRANS_NOTVALID
+    assert _mk(engine, "cufinufftf", 1, 1, (10, 0, 15)) == 0  # higher dims ignored
+    o = _lib.default_opts()
+    o.upsampfac, o.gpu_kerevalmeth = 0.9, 1
+    assert _mk(engine, "cufinufftf", 1, 2, N, opts=o) == 8  # FINUFFT_ERR_HORNER_WRONG_BETA
+    o.gpu_kerevalmeth = 0
+    assert _mk(engine, "cufinufftf", 1, 2, N, opts=o) == 7  # FINUFFT_ERR_UPSAMPFAC_TOO_SMALL
+    o.upsampfac = 4.5
+    assert _mk(engine, "cufinufftf", 1, 2, N, opts=o) == 0  # only a warning
+    o = _lib.default_opts()
+    o.gpu_device_id = 999
+    assert _mk(engine, "cufinufftf", 1, 2, N, opts=o) == 15  # FINUFFT_ERR_CUDA_FAILURE
+    o = _lib.default_opts()
+    o.gpu_method, o.gpu_binsizex, o.gpu_binsizey, o.gpu_binsizez = 2, 200, 200, 200
+    assert _mk(engine, "cufinufftf", 1, 3, (64, 64, 64), opts=o) == 19  # INSUFFICIENT_SHMEM
+
+
+def test_type3_null_targets(engine):
+    import torch
+
+    p = ctypes.c_void_p()
+    assert engine.cufinufftf_makeplan(3, 2, None, 1, 1, 1e-5, ctypes.byref(p), None) == 0
+    x = torch.zeros(10, device="cuda")
+    ier = engine.cufinufftf_setpts(p, 10, x.data_ptr(), x.data_ptr(), None, 5, x.data_ptr(),
+                                   None, None)
+    assert ier == 21  # FINUFFT_ERR_INVALID_ARGUMENT
+    assert engine.cufinufftf_destroy(p) == 0
+
+
+@pytest.mark.parametrize("ty", [1, 2, 3])
+def test_many_vectors_partial_batch(oracle, ty):
+    """ntransf=5 with batches of 2 (last batch partial) equals 5 single transforms."""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(7)
+    nm, M, nt = (24, 32), 3000, 5
+    pts = rng.uniform(-np.pi, np.pi, (2, M)).astype(np.float32)
+    freq = rng.uniform(-20, 20, (2, 700)).astype(np.float32)
+    extra = [_dev(f) for f in freq] if ty == 3 else []
+    many = fg.Plan(ty, 2 if ty == 3 else nm, n_trans=nt, eps=1e-5, gpu_maxbatchsize=2)
+    many.setpts(*[_dev(p) for p in pts], *extra)
+    one = fg.Plan(ty, 2 if ty == 3 else nm, n_trans=1, eps=1e-5)
+    one.setpts(*[_dev(p) for p in pts], *extra)
+    data = _cx(rng, (nt, M) if ty != 2 else (nt,) + nm)
+    out = many.execute(_dev(data)).cpu().numpy()
+    for t in range(nt):
+        ref = one.execute(_dev(data[t])).cpu().numpy()
+        assert oracle.rel_l2(out[t], ref) < 1e-6
+
+
+def test_modeord_fft_order(oracle):
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(8)
+    nm, M = (15, 16), 2000
+    pts = rng.uniform(-np.pi, np.pi, (2, M)).astype(np.float32)
+    c = _cx(rng, M)
+    p0 = fg.Plan(1, nm, eps=1e-5)
+    p1 = fg.Plan(1, nm, eps=1e-5, modeord=1)
+    for p in (p0, p1):
+        p.setpts(*[_dev(q) for q in pts])
+    f0 = p0.execute(_dev(c)).cpu().numpy()
+    f1 = p1.execute(_dev(c)).cpu().numpy()
+    np.testing.assert_allclose(np.fft.ifftshift(f0), f1, rtol=0, atol=1e-5 * np.abs(f0).max())
+    # type 2 reads modes in FFT order
+    fk = _cx(rng, nm)
+    q0, q1 = fg.Plan(2, nm, eps=1e-5), fg.Plan(2, nm, eps=1e-5, modeord=1)
+    for p in (q0, q1):
+        p.setpts(*[_dev(q) for q in pts])
+    a = q0.execute(_dev(fk)).cpu().numpy()
+    b = q1.execute(_dev(np.fft.ifftshift(fk))).cpu().numpy()
+    assert oracle.rel_l2(b, a) < 1e-6
+
+
+def test_spreadinterponly(oracle):
+    """gpu_spreadinterponly: type 1 spreads onto the mode grid itself, type 2
+    interpolates from it (no FFT, no deconvolution)."""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(9)
+    nm, M = (64, 48), 4000
+    pts = rng.uniform(-np.pi, np.pi, (2, M)).astype(np.float64)
+    c = _cx(rng, M, "complex128")
+    p = fg.Plan(1, nm, eps=1e-10, dtype="complex128", gpu_spreadinterponly=1)
+    p.setpts(*[_dev(q) for q in pts])
+    g = p.execute(_dev(c)).cpu().numpy()
+    ns, beta = oracle.gpu_kernel(1e-10, 2.0, 1, False)
+    ref = oracle._spread(_oracle_pts(pts), c, list(nm[::-1]), ns, beta)
+    assert oracle.rel_l2(g, ref) < 1e-12
+    q = fg.Plan(2, nm, eps=1e-10, dtype="complex128", gpu_spreadinterponly=1)
+    q.setpts(*[_dev(x) for x in pts])
+    got = q.execute(_dev(ref)).cpu().numpy()
+    want = oracle._interp(_oracle_pts(pts), ref, list(nm[::-1]), ns, beta)
+    assert oracle.rel_l2(got, want) < 1e-12
+
+
+def _oracle_pts(pts):
+    return [p.astype(np.float64) for p in pts[::-1]]
+
+
+@pytest.mark.parametrize("ty", [1, 2, 3])
+@pytest.mark.parametrize("dtype", ["complex64", "complex128"])
+def test_adjointness(ty, dtype):
+    """<A x, y> = <x, A* y> (test/adjointness.cpp): tol 1e-6 float, 1e-12 double."""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(10 + ty)
+    rdt = np.float32 if dtype == "complex64" else np.float64
+    nm, M = (20, 16, 12), 2500
+    pts = rng.uniform(-np.pi, np.pi, (3, M)).astype(rdt)
+    freq = rng.uniform(-15, 15, (3, 900)).astype(rdt)
+    extra = [_dev(f) for f in freq] if ty == 3 else []
+    tol = 1e-6 if dtype == "complex64" else 1e-12
+    p = fg.Plan(ty, 3 if ty == 3 else nm, eps=tol, dtype=dtype)
+    p.setpts(*[_dev(q) for q in pts], *extra)
+    nout = (900,) if ty == 3 else nm
+    x = _cx(rng, (M,) if ty != 2 else nm, dtype)
+    y = _cx(rng, nout if ty != 2 else (M,), dtype)
+    ax = p.execute(_dev(x)).cpu().numpy().astype(np.complex128)
+    aty = p.execute_adjoint(_dev(y)).cpu().numpy().astype(np.complex128)
+    lhs = np.vdot(y.ravel(), ax.ravel())
+    rhs = np.vdot(aty.ravel(), x.ravel())
+    assert abs(lhs - rhs) / abs(lhs) < (1e-5 if dtype == "complex64" else 1e-11)
+
+
+@pytest.mark.parametrize("prec", ["f", ""])
+def test_host_pointer_api(oracle, engine, prec):
+    """finufft[f]_makeplan/setpts/execute/execute_adjoint with host arrays."""
+    from finufft_gb300 import _lib
+
+    rdt = np.float32 if prec == "f" else np.float64
+    cdt = np.complex64 if prec == "f" else np.complex128
+    pfx = "finufft" + prec
+    rng = np.random.default_rng(11)
+    M, nm = 3000, (18, 14)  # C order: n_modes[0] fastest
+    x, y = rng.uniform(-np.pi, np.pi, (2, M)).astype(rdt)
+    c = _cx(rng, M, cdt)
+    p = ctypes.c_void_p()
+    tol = 1e-5 if prec == "f" else 1e-11
+    m = (ctypes.c_int64 * 3)(nm[0], nm[1], 1)
+    assert getattr(engine, pfx + "_makeplan")(1, 2, m, 1, 1, tol, ctypes.byref(p), None) == 0
+    assert getattr(engine, pfx + "_setpts")(p, M, x.ctypes.data, y.ctypes.data, None, 0, None,
+                                            None, None) == 0
+    f = np.zeros(nm[0] * nm[1], dtype=cdt)
+    assert getattr(engine, pfx + "_execute")(p, c.ctypes.data, f.ctypes.data) == 0
+    ref = oracle.dirft1([x, y], c, 1, nm)
+    assert oracle.rel_l2(f, ref) < 20 * tol
+    # adjoint of type 1 = type 2 with the opposite sign, modes -> points
+    g = _cx(rng, nm[0] * nm[1], cdt)
+    cc = np.zeros(M, dtype=cdt)
+    assert getattr(engine, pfx + "_execute_adjoint")(p, cc.ctypes.data, g.ctypes.data) == 0
+    assert oracle.rel_l2(cc, oracle.dirft2([x, y], g, -1, nm)) < 20 * tol
+    assert getattr(engine, pfx + "_destroy")(p) == 0
+
+
+def test_simple_interfaces(oracle, engine):
+    import torch
+
+    rng = np.random.default_rng(12)
+    M = 2000
+    x, y, z = rng.uniform(-np.pi, np.pi, (3, M)).astype(np.float32)
+    c = _cx(rng, M)
+    fk = torch.zeros(8 * 6 * 4, dtype=torch.complex64, device="cuda")
+    d = [_dev(a) for a in (x, y, z, c)]
+    ier = engine.cufinufftf3d1(ctypes.c_int64(M), ctypes.c_void_p(d[0].data_ptr()),
+                               ctypes.c_void_p(d[1].data_ptr()), ctypes.c_void_p(d[2].data_ptr()),
+                               ctypes.c_void_p(d[3].data_ptr()), 1, ctypes.c_float(1e-5),
+                               ctypes.c_int64(8), ctypes.c_int64(6), ctypes.c_int64(4),
+                               ctypes.c_void_p(fk.data_ptr()), None)
+    assert ier == 0
+    ref = oracle.dirft1([x, y, z], c, 1, (8, 6, 4))
+    assert oracle.rel_l2(fk.cpu().numpy(), ref) < 2e-4
+    out = torch.zeros(M, dtype=torch.complex64, device="cuda")
+    ier = engine.cufinufftf1d2(ctypes.c_int64(M), ctypes.c_void_p(d[0].data_ptr()),
+                               ctypes.c_void_p(out.data_ptr()), -1, ctypes.c_float(1e-5),
+                               ctypes.c_int64(48), ctypes.c_void_p(fk.data_ptr()), None)
+    assert ier == 0
+    ref2 = oracle.dirft2([x], fk.cpu().numpy(), -1, (48,))
+    assert oracle.rel_l2(out.cpu().numpy(), ref2) < 2e-4
+
+
+def test_graph_replay_matches_execute(oracle):
+    import torch
+
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(13)
+    nm, M = (32, 32, 32), 50000
+    pts = rng.uniform(-np.pi, np.pi, (3, M)).astype(np.float32)
+    s = torch.cuda.Stream()
+    p = fg.Plan(1, nm, n_trans=3, eps=1e-5, gpu_stream=s.cuda_stream)
+    p.setpts(*[_dev(q) for q in pts])
+    c = _dev(_cx(rng, (3, M)))
+    ref = p.execute(c)
+    torch.cuda.synchronize()
+    out = torch.zeros_like(ref)
+    p.graph_capture(c, out)
+    for _ in range(3):
+        p.graph_launch()
+    torch.cuda.synchronize()
+    assert oracle.rel_l2(out.cpu().numpy(), ref.cpu().numpy()) < 1e-6
+
+
+@pytest.mark.parametrize("ty", [1, 2])
+def test_edge_cases(oracle, ty):
+    """M=0 gives zeros, single mode, all points in one bin, tiny grids."""
+    import torch
+
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(14)
+    p = fg.Plan(ty, (7, 5), eps=1e-5)
+    e = torch.zeros(0, device="cuda")
+    p.setpts(e, e)
+    if ty == 1:
+        out = p.execute(torch.zeros((1, 0), dtype=torch.complex64, device="cuda"))
+        assert out.abs().max().item() == 0
+    else:
+        out = p.execute(_dev(_cx(rng, (7, 5))))
+        assert out.numel() == 0
+    # one mode, tiny grid, a dense cluster in one bin, points on the seam
+    M = 20000
+    pts = np.full((2, M), 0.5, np.float32) + 1e-3 * rng.standard_normal((2, M)).astype(np.float32)
+    pts[:, :10] = np.float32(np.pi)
+    for nm in [(1, 1), (2, 3), (64, 64)]:
+        q = fg.Plan(ty, nm, eps=1e-5)
+        q.setpts(*[_dev(a) for a in pts])
+        if ty == 1:
+            c = _cx(rng, M)
+            f = q.execute(_dev(c)).cpu().numpy()
+            ref = oracle.dirft1(_oracle_pts(pts), c, 1, nm[::-1]).reshape(nm)
+        else:
+            fk = _cx(rng, nm)
+            f = q.execute(_dev(fk)).cpu().numpy()
+            ref = oracle.dirft2(_oracle_pts(pts), fk.ravel(), -1, nm[::-1])
+        assert oracle.rel_l2(f, ref) < 1e-3

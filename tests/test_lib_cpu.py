@@ -1,0 +1,96 @@
+"""CPU checks of the C-ABI library: it loads, exports every entry point that
+include/*.h declares, and its host-only paths (option defaults, argument
+validation that precedes any device work) behave as the reference's."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = ["cufinufft.h", "finufft.h", "gbnufft_ext.h"]
+
+
+def declared_symbols():
+    """Names declared with GBNUFFT_EXPORT, found by preprocessing the headers."""
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    names = set()
+    for h in HEADERS:
+        src = '#define GBNUFFT_EXPORT __gbx__\n#include "%s"\n' % h
+        out = subprocess.run(["gcc", "-E", "-P", "-x", "c", "-I", os.path.join(ROOT, "include"),
+                              "-I", cuda_inc, "-"], input=src, capture_output=True, text=True,
+                             check=True).stdout
+        names |= set(re.findall(r"__gbx__[^;(]*?\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", out))
+        names |= set(re.findall(r"__gbx__\s+extern\s+const\s+int\s+([A-Za-z_][A-Za-z0-9_]*)", out))
+    return sorted(names)
+
+
+def test_headers_declare_the_reference_surface():
+    names = declared_symbols()
+    cu = [n for n in names if n.startswith("cufinufft")]
+    # 45 cufinufft* symbols of the reference (include/cufinufft.h) + 12 extensions
+    base = [n for n in cu if not re.search(r"(adjoint|plan_info|stage_times|get_sort|graph_)", n)]
+    assert len(base) == 45
+    host = [n for n in names if n.startswith("finufft")]
+    assert len(host) == 12 + 36  # guru (6 x 2) + simple (18 x 2)
+    assert "FINUFFT_FFT_DEFAULT" in names
+
+
+def test_library_exports_every_declared_symbol(engine):
+    missing = [n for n in declared_symbols() if not hasattr(engine, n)]
+    assert missing == []
+
+
+def test_cufinufft_default_opts(engine):
+    from finufft_gb300 import _lib
+
+    o = _lib.default_opts()
+    # src/cuda/c_interface.cpp:151-173
+    assert o.gpu_method == 0 and o.gpu_sort == 1 and o.gpu_kerevalmeth == 1
+    assert o.upsampfac == 0.0 and o.gpu_maxsubprobsize == 1024 and o.gpu_maxbatchsize == 0
+    assert o.gpu_binsizex == o.gpu_binsizey == o.gpu_binsizez == 0
+    assert o.modeord == 0 and o.gpu_spreadinterponly == 0 and o.gpu_np == 0 and o.debug == 0
+    assert ctypes.sizeof(o) == 88  # 8 + 13 ints, pad, stream pointer, 3 ints, pad
+
+
+def test_finufft_default_opts(engine):
+    from finufft_gb300 import _lib
+
+    o = _lib.FinufftOpts()
+    engine.finufft_default_opts(ctypes.byref(o))
+    assert o.showwarn == 1 and o.spread_sort == 2 and o.spread_nthr_atomic == -1
+    assert o.upsampfac == 0.0 and o.maxbatchsize == 0 and o.allow_eps_too_small == 0
+
+
+def _mk(engine, pfx, ty, dim, modes, ntr=1, tol=1e-6):
+    p = ctypes.c_void_p()
+    m = (ctypes.c_int64 * 3)(*modes)
+    fn = getattr(engine, pfx + "_makeplan")
+    return fn(ty, dim, m, 1, ntr, tol, ctypes.byref(p), None)
+
+
+@pytest.mark.parametrize("pfx", ["cufinufft", "cufinufftf"])
+def test_device_api_host_side_errors(engine, pfx):
+    # test/cuda/test_makeplan.c: checks that precede any device work
+    assert _mk(engine, pfx, 1, 0, (10, 20, 15)) == 12  # FINUFFT_ERR_DIM_NOTVALID
+    assert _mk(engine, pfx, 1, 4, (10, 20, 15)) == 12
+    assert _mk(engine, pfx, 1, 1, (0, 20, 15)) == 14  # FINUFFT_ERR_NDATA_NOTVALID
+    assert _mk(engine, pfx, 1, 1, (2 ** 31, 1, 1)) == 14
+    assert _mk(engine, pfx, 1, 2, (10, 0, 1)) == 14
+    assert _mk(engine, pfx, 1, 2, (2 ** 31 - 1, 2, 1)) == 14
+    assert _mk(engine, pfx, 1, 3, (10, 15, 0)) == 14
+    assert _mk(engine, pfx, 1, 3, (2 ** 30, 2, 2)) == 14
+    assert getattr(engine, pfx + "_destroy")(None) == 16  # FINUFFT_ERR_PLAN_NOTVALID
+    assert getattr(engine, pfx + "_setpts")(None, 10, None, None, None, 0, None, None, None) == 16
+    assert getattr(engine, pfx + "_setpts")(None, 2 ** 31, None, None, None, 0, None, None, None) == 14
+    assert getattr(engine, pfx + "_execute")(None, None, None) == 16
+
+
+@pytest.mark.parametrize("pfx", ["finufft", "finufftf"])
+def test_host_api_host_side_errors(engine, pfx):
+    assert _mk(engine, pfx, 4, 1, (10, 1, 1)) == 10  # FINUFFT_ERR_TYPE_NOTVALID
+    assert _mk(engine, pfx, 1, 0, (10, 1, 1)) == 12
+    assert _mk(engine, pfx, 1, 1, (10, 1, 1), ntr=0) == 9  # FINUFFT_ERR_NTRANS_NOTVALID
+    assert _mk(engine, pfx, 1, 1, (10, 1, 1), tol=1e-30) == 26  # FINUFFT_ERR_EPS_TOO_SMALL
+    assert getattr(engine, pfx + "_destroy")(None) == 16

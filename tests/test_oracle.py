@@ -1,0 +1,156 @@
+"""CPU tests of the oracle: pinned to the reference's own code (golden
+fixtures generated by tests/golden/make_golden.py from the reference's
+src/common) and to FP64 direct sums."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "reference_planning.json")
+
+
+@pytest.fixture(scope="module")
+def gold():
+    with open(GOLD) as f:
+        return json.load(f)
+
+
+def test_next235_against_reference(oracle, gold):
+    for n, v in gold["next235_even"]:
+        assert oracle.next235_even(n) == v, n
+
+
+def test_next235_known_answers(oracle):
+    # the true outputs next235(n, 2) for n = 0..20 (test/testutils.cpp:39-44)
+    want = [2, 2, 2, 4, 4, 6, 6, 8, 8, 10, 10, 12, 12, 16, 16, 16, 16, 18, 18, 20, 20]
+    assert [oracle.next235_even(n) for n in range(21)] == want
+    assert oracle.next235_even(3 * 10 ** 9) >= 3 * 10 ** 9
+
+
+def test_gauss_legendre_against_reference(oracle, gold):
+    for n, (x, w) in gold["gaussquad"].items():
+        xx, ww = oracle.gauss_legendre(int(n))
+        np.testing.assert_allclose(xx, x, atol=1e-15)
+        np.testing.assert_allclose(ww, w, rtol=1e-13, atol=5e-15)
+
+
+def test_gauss_legendre_integrates(oracle):
+    # test/testutils.cpp:73-85: 16 nodes integrate f' exactly to 1e-14
+    x, w = oracle.gauss_legendre(16)
+    f = lambda t: np.sin(4 * t + 1.0) + 0.3
+    fp = lambda t: 4 * np.cos(4 * t + 1.0)
+    assert abs(np.dot(w, fp(x)) - (f(1.0) - f(-1.0))) < 1e-14
+
+
+def test_type3_grid_against_reference(oracle, gold):
+    for s, X, S, ns, nf, h, gam in gold["nhg_type3"]:
+        a, b, c = oracle.type3_grid(s, X, S, ns)
+        assert a == nf
+        assert b == pytest.approx(h, rel=1e-15)
+        assert c == pytest.approx(gam, rel=1e-14)
+
+
+def test_cpu_kernel_shape_against_reference(oracle, gold):
+    for tol, dim, ty, s, ns, beta in gold["cpu_kernel"]:
+        n2, b2 = oracle.cpu_kernel(tol, dim, ty, s, clip=False)
+        assert n2 == ns
+        assert b2 == pytest.approx(beta, rel=1e-14)
+
+
+def test_pswf_against_reference(oracle, gold):
+    z = np.array(gold["pswf"]["z"])
+    for c, v in gold["pswf"]["values"].items():
+        np.testing.assert_allclose(oracle.pswf0(float(c), z), v, atol=2e-15)
+
+
+def test_gpu_kernel_rule(oracle):
+    # widths/betas of the GPU rule (src/cuda/makeplan.cu:91-115) at the metric configs
+    assert oracle.gpu_kernel(1e-5, 2.0, 1, True) == (6, pytest.approx(13.8, rel=1e-6))
+    ns, beta = oracle.gpu_kernel(1e-12, 2.0, 1, False)
+    assert ns == 13 and beta == pytest.approx(29.9)
+    assert oracle.gpu_kernel(1e-6, 1.25, 1, True)[0] == 10
+    assert oracle.gpu_kernel(1e-1, 2.0, 1, True)[0] == 2
+    assert oracle.gpu_kernel(1e-16, 2.0, 1, False)[0] == 16  # clipped
+    with pytest.raises(ValueError, match="8"):
+        oracle.gpu_kernel(1e-5, 1.5, 1, True)
+    with pytest.raises(ValueError, match="7"):
+        oracle.gpu_kernel(1e-5, 0.9, 0, True)
+
+
+def test_dirft_small_against_numpy(oracle):
+    rng = np.random.default_rng(0)
+    x, y = rng.uniform(-np.pi, np.pi, (2, 7))
+    c = rng.standard_normal(7) + 1j * rng.standard_normal(7)
+    nm = (4, 3)
+    f = oracle.dirft1([x, y], c, -1, nm).reshape(3, 4)
+    k1 = np.arange(4) - 2
+    k2 = np.arange(3) - 1
+    want = np.array([[np.sum(c * np.exp(-1j * (a * x + b * y))) for a in k1] for b in k2])
+    np.testing.assert_allclose(f, want, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+@pytest.mark.parametrize("ty", [1, 2, 3])
+def test_es_restatement_against_dirft(oracle, dim, ty):
+    rng = np.random.default_rng(dim * 10 + ty)
+    M = 200
+    nm = [16, 12, 10][:dim]
+    xs = [rng.uniform(-np.pi, np.pi, M) for _ in range(dim)]
+    c = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    tol = 1e-9 if ty != 3 else 1e-6
+    if ty == 1:
+        got = oracle.nufft_es(1, xs, c, 1, tol, n_modes=nm, is_float=False)
+        ref = oracle.dirft1(xs, c, 1, nm)
+    elif ty == 2:
+        fk = rng.standard_normal(tuple(reversed(nm))) + 1j * rng.standard_normal(tuple(reversed(nm)))
+        got = oracle.nufft_es(2, xs, fk, -1, tol, n_modes=nm, is_float=False)
+        ref = oracle.dirft2(xs, fk, -1, nm)
+    else:
+        ss = [rng.uniform(-30, 30, 60) for _ in range(dim)]
+        got = oracle.nufft_es(3, xs, c, 1, tol, ss=ss, is_float=False)
+        ref = oracle.dirft3(xs, c, 1, ss)
+    assert oracle.rel_l2(got, ref) < 10 * tol
+
+
+@pytest.mark.parametrize("ty", [1, 2])
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-9), (np.complex64, 1e-4)])
+def test_cpu_pswf_restatement_against_dirft(oracle, ty, dtype, tol):
+    rng = np.random.default_rng(5)
+    M, nm = 500, [20, 16, 12]
+    xs = [rng.uniform(-np.pi, np.pi, M) for _ in range(3)]
+    plan = oracle.CpuPlan(ty, nm, 1 if ty == 1 else -1, tol, dtype=dtype)
+    plan.setpts(xs)
+    if ty == 1:
+        c = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+        err = oracle.rel_l2(plan.execute(c), oracle.dirft1(xs, c, 1, nm))
+    else:
+        fk = rng.standard_normal((12, 16, 20)) + 1j * rng.standard_normal((12, 16, 20))
+        err = oracle.rel_l2(plan.execute(fk), oracle.dirft2(xs, fk, -1, nm))
+    assert err < (10 * tol if dtype == np.complex128 else 5 * tol)
+
+
+def test_bin_sort_is_stable_and_bin_ordered(oracle):
+    rng = np.random.default_rng(3)
+    M = 5000
+    xs = [rng.uniform(-np.pi, np.pi, M) for _ in range(3)]
+    xs[0][:10] = np.pi  # exactly on the periodic seam
+    xs[1][10:20] = -np.pi
+    nf, bins = [40, 30, 20], [8, 7, 6]
+    perm, loc = oracle.bin_sort(xs, nf, bins)
+    assert sorted(perm.tolist()) == list(range(M))
+    # loc lies in [0, bin]
+    for d in range(3):
+        assert loc[d].min() >= 0 and loc[d].max() <= bins[d]
+    # stability: within runs of equal bins, input indices increase
+    nb = [(nf[d] + bins[d] - 1) // bins[d] for d in range(3)]
+    cell = []
+    for d in range(3):
+        r = np.mod(xs[d] / (2 * np.pi) + 0.5, 1.0) * nf[d]
+        cell.append(np.minimum(np.floor(r).astype(int), nf[d] - 1) // bins[d])
+    key = cell[0] + nb[0] * (cell[1] + nb[1] * cell[2])
+    ks = key[perm]
+    # away from float ties the numpy key agrees with the exact fold
+    assert np.mean(np.diff(ks) >= 0) > 0.999
+    same = np.diff(ks) == 0
+    assert np.all(np.diff(perm)[same] > 0)
