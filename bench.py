@@ -162,6 +162,10 @@ def run_gpu(args):
     torch.cuda.synchronize()
     st = plain.stage_times(True)
     info = plain.info()
+    if args.only == "plain":
+        print(json.dumps({"plain_ms": ms_plain, "stage_ms": st, "M": M, "nsub": info.nsub,
+                          "bins": list(info.bins)}))
+        return
     del plain
     torch.cuda.empty_cache()
 
@@ -329,6 +333,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4_000_000)
     ap.add_argument("--err-modes", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", default="", choices=["", "plain"],
+                    help="plain: time only the single-transform plan (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -40,6 +40,7 @@ struct Error {
   do {                                                                                   \
     cudaError_t e_ = (call);                                                             \
     if (e_ != cudaSuccess) {                                                             \
+      cudaGetLastError(); /* clear a non-sticky error so it does not leak to the caller */ \
       fprintf(stderr, "[gbnufft] CUDA error %s at %s:%d\n", cudaGetErrorString(e_),      \
               __FILE__, __LINE__);                                                       \
       throw ::gbn::Error{FINUFFT_ERR_CUDA_FAILURE, cudaGetErrorString(e_)};              \

@@ -5,6 +5,7 @@
 #include "device_util.cuh"
 #include "elementwise.h"
 #include "spreadinterp.h"
+#include "tile_layout.h"
 
 namespace gbn {
 
@@ -16,17 +17,16 @@ template <typename T, int DIM>
 void interp_dim(const PointLayout<T> &, const KernelShape<T> &, const cplx<T> *, int64_t,
                 const cplx<T> *, int, cplx<T> *, int, cudaStream_t);
 
-template <typename T> size_t spread_tile_smem(int dim, int ns, const int bin[3]) {
-  auto pitch = [&](int tx) {
-    return dim == 3 ? (tx <= 8 ? 8 : 16 * ((tx - 8 + 15) / 16) + 8) : tx;
-  };
-  size_t cells = (size_t)pitch(bin[0] + ns);
+template <typename T> size_t spread_tile_smem(int dim, int ns, const int bin[3], int threads) {
+  if (dim == 3) // tile (padded pitches) + per-warp staging of 32 points
+    return tile3_bytes<T>(ns, bin[0], bin[1], bin[2]) +
+           (size_t)(threads / 32) * stage_bytes_per_warp<T>(ns);
+  size_t cells = (size_t)(bin[0] + ns);
   if (dim > 1) cells *= (size_t)(bin[1] + ns);
-  if (dim > 2) cells *= (size_t)(bin[2] + ns);
   return 2 * sizeof(T) * cells;
 }
-template size_t spread_tile_smem<float>(int, int, const int[3]);
-template size_t spread_tile_smem<double>(int, int, const int[3]);
+template size_t spread_tile_smem<float>(int, int, const int[3], int);
+template size_t spread_tile_smem<double>(int, int, const int[3], int);
 
 template <typename T>
 void launch_spread(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *c,

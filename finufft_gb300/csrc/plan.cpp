@@ -116,13 +116,17 @@ template <typename T> Plan<T>::~Plan() {
 }
 
 template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
-  // bins: user value, else a default of this engine per dimension and width
+  // bins: the user's values, else this engine's defaults per dimension
   const int ns = K.ns;
-  int def = 1024;
-  if (dim == 2) def = 32;
-  if (dim == 3) {
-    const int tile = (std::is_same_v<T, float> ? (ns <= 8 ? 16 : 24) : (ns <= 8 ? 16 : 20));
-    def = std::max(4, tile - ns);
+  const int limit = max_smem_optin(opts.gpu_device_id);
+  const int threads = (dim == 3 && !std::is_same_v<T, float>) ? 128 : 256;
+  int def = dim == 1 ? 1024 : (dim == 2 ? 32 : 8);
+  if (dim == 3) { // largest even bin (<= 8) whose tile and staging fit in shared memory
+    while (def > 2) {
+      const int b3[3] = {def, def, def};
+      if (spread_tile_smem<T>(3, ns, b3, threads) <= (size_t)limit) break;
+      def -= 2;
+    }
   }
   bins[0] = opts.gpu_binsizex > 0 ? opts.gpu_binsizex : def;
   bins[1] = dim > 1 ? (opts.gpu_binsizey > 0 ? opts.gpu_binsizey : def) : 1;
@@ -131,10 +135,11 @@ template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
     if (d >= dim) bins[d] = 1;
     nbins[d] = d < dim ? ceil_div(nf[d], bins[d]) : 1;
   }
+  if (dim == 3 && (bins[0] > 1000 || bins[1] > 1000 || bins[2] > 1000))
+    GBN_THROW(FINUFFT_ERR_BINSIZE_NOTVALID, "3D bins must be < 1000");
   if (opts.gpu_maxsubprobsize < 1) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "maxsubprobsize");
   method = opts.gpu_method == 0 ? 2 : (opts.gpu_method == 1 ? 1 : 2);
-  spread_smem = spread_tile_smem<T>(dim, ns, bins);
-  const int limit = max_smem_optin(opts.gpu_device_id);
+  spread_smem = spread_tile_smem<T>(dim, ns, bins, threads);
   if (method == 2 && spread_smem > (size_t)limit) {
     if (user_method) {
       fprintf(stderr, "[gbnufft] tile needs %zu bytes of shared memory, %d available\n",
@@ -144,7 +149,7 @@ template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
     method = 1;
   }
   scfg.method = method;
-  scfg.threads = 256;
+  scfg.threads = threads;
   scfg.smem = method == 2 ? spread_smem : 0;
 }
 

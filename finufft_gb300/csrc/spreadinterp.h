@@ -11,7 +11,7 @@ struct SpreadConfig {
 };
 
 // Shared-memory bytes of the tiled spread for a given tile and kernel width.
-template <typename T> size_t spread_tile_smem(int dim, int ns, const int bin[3]);
+template <typename T> size_t spread_tile_smem(int dim, int ns, const int bin[3], int threads);
 
 // fw[t*nf + g] += sum_j c[t*M + j] (* pre[j] or conj(pre[j])) phi(g - x_j), t < ntr.
 // fw must be zeroed by the caller.

@@ -10,6 +10,7 @@
 #pragma once
 #include "device_util.cuh"
 #include "spreadinterp.h"
+#include "tile_layout.h"
 
 namespace gbn {
 
@@ -39,12 +40,6 @@ __device__ __forceinline__ TileGeom<DIM> tile_of(const PointLayout<T> &L, int b)
     g.cells *= g.t[d];
   }
   return g;
-}
-
-// x pitch of the shared tile: in 3D a multiple of 16 plus 8 words, so the four
-// rows an 8 x 4 lane patch touches start in disjoint bank octets.
-__host__ __device__ constexpr int tile_pitch_x(int dim, int tx) {
-  return dim == 3 ? (tx <= 8 ? 8 : 16 * ((tx - 8 + 15) / 16) + 8) : tx;
 }
 
 // periodic wrap of a global index that may be slightly outside [0, n)
@@ -181,10 +176,131 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Method 2 in 3D: tiled spreading with warp-cooperative, bank-conflict-free
+// shared-memory atomics.
+//  * Each warp takes 32 points at a time: lane l loads point l (coalesced),
+//    evaluates its 3*NS kernel weights once and stages them, the start cell
+//    and the strength in a per-warp shared-memory area.
+//  * The warp then adds the 32 points one after another. Lane (lx, lp) =
+//    (lane & 7, lane >> 3) covers x offset dx = 8*xb + lx and the (y, z)
+//    offset pair number 4*r + lp of the NS*NS pairs, i.e. an 8-cell x run
+//    for 4 consecutive (y, z) pairs per instruction (75% of lanes busy at
+//    NS = 6, against 56% for a fixed 8 x 4 (x, y) patch).
+//  * Pitches are chosen so those 32 cells sit in 32 distinct banks: the x
+//    pitch px is 8 mod 16 and the y extent is padded to py = NS mod 4, which
+//    makes the word offset of pair p congruent to px*p mod 32.
+// Returns of the kernel are identical to the other spreaders up to the
+// order of floating-point additions.
+template <typename T, int NS>
+__global__ void __launch_bounds__(256)
+    spread_tile3_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
+                        const cplx<T> *__restrict__ pre, int conj_pre,
+                        cplx<T> *__restrict__ fw, int64_t nf_total) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int SK = STAGE_STRIDE;
+  constexpr int NXB = (NS + 7) / 8;
+  constexpr int NPAIR = NS * NS;
+  constexpr int NROUND = (NPAIR + 3) / 4;
+  const int sub = blockIdx.x;
+  const int tr = blockIdx.y;
+  const int b = L.sub_bin[sub];
+  const int p0 = L.sub_start[sub];
+  const int np = L.sub_count[sub];
+  const TileGeom<3> G = tile_of<T, 3, NS>(L, b);
+  const int px = tile_pitch_x(3, G.t[0]);
+  const int py = tile3_py(G.t[1], NS);
+  const int Q = px * py;
+  const int ncell = Q * G.t[2];
+  T *re = reinterpret_cast<T *>(smem_raw);
+  T *im = re + ncell;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  unsigned char *stage = smem_raw + tile3_bytes<T>(NS, L.bin[0], L.bin[1], L.bin[2]) +
+                         (size_t)warp * stage_bytes_per_warp<T>(NS);
+  T *kx = reinterpret_cast<T *>(stage);
+  T *ky = kx + NS * SK;
+  T *kz = ky + NS * SK;
+  T *vre = kz + NS * SK;
+  T *vim = vre + SK;
+  int *spk = reinterpret_cast<int *>(vim + SK);
+  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+    re[i] = T(0);
+    im[i] = T(0);
+  }
+  __syncthreads();
+  const cplx<T> *ct = c + (int64_t)tr * L.M;
+  const int lx = lane & 7, lp = lane >> 3;
+  for (int base = warp * 32; base < np; base += nwarp * 32) {
+    const int i = base + lane;
+    if (i < np) {
+      const int p = p0 + i;
+      const int j = L.perm[p];
+      cplx<T> v = ct[j];
+      if (pre) v = cmul_opt<T>(v, pre[j], conj_pre);
+      T kk[NS];
+      const int sx = point_weights<T, NS>(L.loc[0][p], L.bin[0], K, kk);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) kx[a * SK + lane] = kk[a];
+      const int sy = point_weights<T, NS>(L.loc[1][p], L.bin[1], K, kk);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) ky[a * SK + lane] = kk[a];
+      const int sz = point_weights<T, NS>(L.loc[2][p], L.bin[2], K, kk);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) kz[a * SK + lane] = kk[a];
+      vre[lane] = v.x;
+      vim[lane] = v.y;
+      spk[lane] = sx | (sy << 10) | (sz << 20);
+    }
+    __syncwarp();
+    const int cnt = min(32, np - base);
+    for (int q = 0; q < cnt; ++q) {
+      const int sp = spk[q];
+      const int rowbase = (sp >> 20) * Q + ((sp >> 10) & 1023) * px + (sp & 1023);
+      const T vr = vre[q], vi = vim[q];
+#pragma unroll
+      for (int xb = 0; xb < NXB; ++xb) {
+        const int dx = xb * 8 + lx;
+        const bool xin = dx < NS;
+        const T wx = kx[dx * SK + q]; // dx >= NS reads (unused) staged y weights
+        const T ar = vr * wx, ai = vi * wx;
+#pragma unroll
+        for (int r = 0; r < NROUND; ++r) {
+          const int pp = 4 * r + lp;
+          if (xin && pp < NPAIR) {
+            const int dy = pp % NS, dz = pp / NS;
+            const T w = ky[dy * SK + q] * kz[dz * SK + q];
+            const int a = rowbase + dz * Q + dy * px + dx;
+            atomicAdd(re + a, ar * w);
+            atomicAdd(im + a, ai * w);
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  for (int q = threadIdx.x; q < G.cells; q += blockDim.x) {
+    const int x = q % G.t[0];
+    const int y = (q / G.t[0]) % G.t[1];
+    const int z = q / (G.t[0] * G.t[1]);
+    const int sidx = z * Q + y * px + x;
+    cplx<T> v;
+    v.x = re[sidx];
+    v.y = im[sidx];
+    const int64_t g = wrap_idx(G.org[0] + x, L.nf[0]) +
+                      (int64_t)L.nf[0] * (wrap_idx(G.org[1] + y, L.nf[1]) +
+                                          (int64_t)L.nf[1] * wrap_idx(G.org[2] + z, L.nf[2]));
+    atomic_add_cplx_global(fwt + g, v);
+  }
+}
+
 // Method 1: point-driven spreading straight into global memory with vector
 // atomics (no tile). Points are still processed in bin order for locality.
+constexpr int GLOBAL_SPREAD_THREADS = 128;
+
 template <typename T, int DIM, int NS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(GLOBAL_SPREAD_THREADS)
     spread_global_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
                          const cplx<T> *__restrict__ pre, int conj_pre,
                          cplx<T> *__restrict__ fw, int64_t nf_total) {
@@ -196,6 +312,8 @@ __global__ void __launch_bounds__(256)
   const TileGeom<DIM> G = tile_of<T, DIM, NS>(L, b);
   const cplx<T> *ct = c + (int64_t)tr * L.M;
   cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  __shared__ T zst[DIM == 3 ? GLOBAL_SPREAD_THREADS * (NS + 1) : 1];
+  __shared__ int zsti[DIM == 3 ? GLOBAL_SPREAD_THREADS * (NS + 1) : 1];
   for (int i = threadIdx.x; i < np; i += blockDim.x) {
     const int p = p0 + i;
     const int j = L.perm[p];
@@ -231,10 +349,17 @@ __global__ void __launch_bounds__(256)
         }
       }
     } else {
+      T *kzs = zst + threadIdx.x * (NS + 1);
+      int *gzs = zsti + threadIdx.x * (NS + 1);
+#pragma unroll
+      for (int cc = 0; cc < NS; ++cc) {
+        kzs[cc] = ker[DIM > 2 ? 2 : 0][cc];
+        gzs[cc] = gi[DIM > 2 ? 2 : 0][cc];
+      }
 #pragma unroll 1
       for (int cc = 0; cc < NS; ++cc) {
-        const int64_t plane = (int64_t)gi[DIM > 2 ? 2 : 0][cc] * L.nf[0] * L.nf[1];
-        const T zr = v.x * ker[DIM > 2 ? 2 : 0][cc], zi = v.y * ker[DIM > 2 ? 2 : 0][cc];
+        const int64_t plane = (int64_t)gzs[cc] * L.nf[0] * L.nf[1];
+        const T zr = v.x * kzs[cc], zi = v.y * kzs[cc];
 #pragma unroll
         for (int bb = 0; bb < NS; ++bb) {
           const int64_t row = plane + (int64_t)gi[DIM > 1 ? 1 : 0][bb] * L.nf[0];
@@ -255,8 +380,10 @@ __global__ void __launch_bounds__(256)
 // ---------------------------------------------------------------------------
 // Interpolation: one thread per point, gathering the NS^DIM support values of
 // the fine grid (read through L1/L2: the points of a subproblem share a tile).
+constexpr int INTERP_THREADS = 128;
+
 template <typename T, int DIM, int NS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(INTERP_THREADS)
     interp_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ fw,
                   int64_t nf_total, const cplx<T> *__restrict__ post, int conj_post,
                   cplx<T> *__restrict__ out) {
@@ -268,6 +395,8 @@ __global__ void __launch_bounds__(256)
   const TileGeom<DIM> G = tile_of<T, DIM, NS>(L, b);
   const cplx<T> *fwt = fw + (int64_t)tr * nf_total;
   cplx<T> *ot = out + (int64_t)tr * L.M;
+  __shared__ T zst[DIM == 3 ? INTERP_THREADS * (NS + 1) : 1];
+  __shared__ int zsti[DIM == 3 ? INTERP_THREADS * (NS + 1) : 1];
   for (int i = threadIdx.x; i < np; i += blockDim.x) {
     const int p = p0 + i;
     const int j = L.perm[p];
@@ -302,9 +431,18 @@ __global__ void __launch_bounds__(256)
         acci = fma(ri, ker[DIM > 1 ? 1 : 0][bb], acci);
       }
     } else {
+      // z weights and rows go through shared memory: a dynamic index into a
+      // register array would put it in local memory
+      T *kzs = zst + threadIdx.x * (NS + 1);
+      int *gzs = reinterpret_cast<int *>(zsti) + threadIdx.x * (NS + 1);
+#pragma unroll
+      for (int cc = 0; cc < NS; ++cc) {
+        kzs[cc] = ker[DIM > 2 ? 2 : 0][cc];
+        gzs[cc] = gi[DIM > 2 ? 2 : 0][cc];
+      }
 #pragma unroll 1
       for (int cc = 0; cc < NS; ++cc) {
-        const int64_t plane = (int64_t)gi[DIM > 2 ? 2 : 0][cc] * L.nf[0] * L.nf[1];
+        const int64_t plane = (int64_t)gzs[cc] * L.nf[0] * L.nf[1];
         T pr = T(0), pi = T(0);
 #pragma unroll
         for (int bb = 0; bb < NS; ++bb) {
@@ -319,8 +457,8 @@ __global__ void __launch_bounds__(256)
           pr = fma(rr, ker[DIM > 1 ? 1 : 0][bb], pr);
           pi = fma(ri, ker[DIM > 1 ? 1 : 0][bb], pi);
         }
-        accr = fma(pr, ker[DIM > 2 ? 2 : 0][cc], accr);
-        acci = fma(pi, ker[DIM > 2 ? 2 : 0][cc], acci);
+        accr = fma(pr, kzs[cc], accr);
+        acci = fma(pi, kzs[cc], acci);
       }
     }
     cplx<T> r;
@@ -339,8 +477,13 @@ template <typename T, int DIM> struct Dispatch {
                      const SpreadConfig &cfg, cudaStream_t s) {
     dim3 grid((unsigned)L.nsub, (unsigned)ntr);
     if (cfg.method == 1) {
-      spread_global_kernel<T, DIM, NS><<<grid, cfg.threads, 0, s>>>(L, K, c, pre, conj_pre, fw,
+      spread_global_kernel<T, DIM, NS><<<grid, GLOBAL_SPREAD_THREADS, 0, s>>>(L, K, c, pre, conj_pre, fw,
                                                                     nf_total);
+    } else if constexpr (DIM == 3) {
+      auto kern = spread_tile3_kernel<T, NS>;
+      GBN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)cfg.smem));
+      kern<<<grid, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
     } else {
       auto kern = spread_tile_kernel<T, DIM, NS>;
       GBN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -354,7 +497,7 @@ template <typename T, int DIM> struct Dispatch {
                      int64_t nf_total, const cplx<T> *post, int conj_post, cplx<T> *out,
                      int ntr, cudaStream_t s) {
     dim3 grid((unsigned)L.nsub, (unsigned)ntr);
-    interp_kernel<T, DIM, NS><<<grid, 128, 0, s>>>(L, K, fw, nf_total, post, conj_post, out);
+    interp_kernel<T, DIM, NS><<<grid, INTERP_THREADS, 0, s>>>(L, K, fw, nf_total, post, conj_post, out);
     GBN_LAUNCH_CHECK();
   }
 };

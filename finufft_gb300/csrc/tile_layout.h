@@ -1,0 +1,28 @@
+// Shared-memory tile geometry of the spreading kernels (host and device).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace gbn {
+
+// x pitch of the shared tile: in 3D a multiple of 16 plus 8 words, so the four
+// rows an 8 x 4 lane patch touches start in disjoint bank octets.
+__host__ __device__ constexpr int tile_pitch_x(int dim, int tx) {
+  return dim == 3 ? (tx <= 8 ? 8 : 16 * ((tx - 8 + 15) / 16) + 8) : tx;
+}
+
+__host__ __device__ constexpr int tile3_py(int ty, int ns) {
+  return ty + (((ns - ty) % 4) + 4) % 4;
+}
+constexpr int STAGE_STRIDE = 33; // padded so 32 lanes write/read distinct banks
+template <typename T> __host__ __device__ constexpr int stage_bytes_per_warp(int ns) {
+  return ((STAGE_STRIDE * (3 * ns + 2) * (int)sizeof(T) + STAGE_STRIDE * 4) + 15) / 16 * 16;
+}
+template <typename T>
+__host__ __device__ constexpr size_t tile3_bytes(int ns, int bx, int by, int bz) {
+  return (2 * sizeof(T) * (size_t)tile_pitch_x(3, bx + ns) * tile3_py(by + ns, ns) * (bz + ns) +
+          15) / 16 * 16;
+}
+
+} // namespace gbn

@@ -75,11 +75,11 @@ def test_many_vectors_partial_batch(oracle, ty):
     nm, M, nt = (24, 32), 3000, 5
     pts = rng.uniform(-np.pi, np.pi, (2, M)).astype(np.float32)
     freq = rng.uniform(-20, 20, (2, 700)).astype(np.float32)
-    extra = [_dev(f) for f in freq] if ty == 3 else []
+    extra = dict(zip('stu', [_dev(f) for f in freq])) if ty == 3 else {}
     many = fg.Plan(ty, 2 if ty == 3 else nm, n_trans=nt, eps=1e-5, gpu_maxbatchsize=2)
-    many.setpts(*[_dev(p) for p in pts], *extra)
+    many.setpts(*[_dev(p) for p in pts], **extra)
     one = fg.Plan(ty, 2 if ty == 3 else nm, n_trans=1, eps=1e-5)
-    one.setpts(*[_dev(p) for p in pts], *extra)
+    one.setpts(*[_dev(p) for p in pts], **extra)
     data = _cx(rng, (nt, M) if ty != 2 else (nt,) + nm)
     out = many.execute(_dev(data)).cpu().numpy()
     for t in range(nt):
@@ -148,10 +148,10 @@ def test_adjointness(ty, dtype):
     nm, M = (20, 16, 12), 2500
     pts = rng.uniform(-np.pi, np.pi, (3, M)).astype(rdt)
     freq = rng.uniform(-15, 15, (3, 900)).astype(rdt)
-    extra = [_dev(f) for f in freq] if ty == 3 else []
+    extra = dict(zip('stu', [_dev(f) for f in freq])) if ty == 3 else {}
     tol = 1e-6 if dtype == "complex64" else 1e-12
     p = fg.Plan(ty, 3 if ty == 3 else nm, eps=tol, dtype=dtype)
-    p.setpts(*[_dev(q) for q in pts], *extra)
+    p.setpts(*[_dev(q) for q in pts], **extra)
     nout = (900,) if ty == 3 else nm
     x = _cx(rng, (M,) if ty != 2 else nm, dtype)
     y = _cx(rng, nout if ty != 2 else (M,), dtype)

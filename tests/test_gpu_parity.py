@@ -97,7 +97,7 @@ def test_type3(oracle, dtype, dim):
     freq = np.stack([rng.uniform(-s, s, N) for s in [40.0, 25.0, 30.0][:dim]]).astype(rdt)
     c = _cx(rng, M, dtype)
     plan = fg.Plan(3, dim, eps=tol, dtype=dtype)
-    plan.setpts(*[_dev(p) for p in pts], *[_dev(s) for s in freq])
+    plan.setpts(*[_dev(p) for p in pts], **dict(zip('stu', [_dev(s) for s in freq])))
     f = plan.execute(_dev(c)).cpu().numpy()
     ref = oracle.dirft3(_oracle_pts(pts), c, 1, _oracle_pts(freq))
     assert oracle.rel_l2(f, ref) < checktol
