@@ -25,6 +25,11 @@ template <typename T> size_t spread_tile_smem(int dim, int ns, const int bin[3],
   if (dim > 1) cells *= (size_t)(bin[1] + ns);
   return 2 * sizeof(T) * cells;
 }
+template <typename T> size_t spread_tile3w_bytes(int ns, const int bin[3]) {
+  return tile3_bytes<T>(ns, bin[0], bin[1], bin[2]) + t3w_stage_bytes(ns, (int)sizeof(T));
+}
+template size_t spread_tile3w_bytes<float>(int, const int[3]);
+template size_t spread_tile3w_bytes<double>(int, const int[3]);
 template size_t spread_tile_smem<float>(int, int, const int[3], int);
 template size_t spread_tile_smem<double>(int, int, const int[3], int);
 

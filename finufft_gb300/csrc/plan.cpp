@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
 #include <limits>
 
 #include "planning.h"
@@ -151,6 +152,19 @@ template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
   scfg.method = method;
   scfg.threads = threads;
   scfg.smem = method == 2 ? spread_smem : 0;
+  scfg.variant = 0;
+  if (dim == 3 && method == 2) {
+    // exclusive-warp tiles when they fit (no atomics, same-cell runs in registers)
+    const size_t wsm = spread_tile3w_bytes<T>(ns, bins);
+    int variant = wsm <= (size_t)limit ? 1 : 0;
+    if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT")) variant = std::atoi(e) == 1 && wsm <= (size_t)limit ? 1 : 0;
+    if (variant == 1) {
+      scfg.variant = 1;
+      scfg.threads = 32;
+      scfg.smem = wsm;
+      spread_smem = wsm;
+    }
+  }
 }
 
 template <typename T> void Plan<T>::make_fft() {
@@ -202,18 +216,23 @@ void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]
   perm.resize(std::max<int64_t>(Mp, 1));
   for (int d = 0; d < dim; ++d) loc[d].resize(std::max<int64_t>(Mp, 1));
   const int nb = nbins[0] * nbins[1] * nbins[2];
+  // keys carry the cell inside the bin when bins * bin volume fits 32 bits
+  const uint64_t binvol = (uint64_t)bins[0] * bins[1] * bins[2];
+  const int cell_keys = (uint64_t)nb * binvol <= 0xffffffffull ? 1 : 0;
+  const uint64_t nkeys = cell_keys ? (uint64_t)nb * binvol : (uint64_t)nb;
   int keybits = 0;
-  while ((1LL << keybits) < nb) ++keybits;
+  while ((1ull << keybits) < nkeys) ++keybits;
   AsyncBuf keys((size_t)std::max<int64_t>(Mp, 1) * 4, stream);
   AsyncBuf skeys((size_t)std::max<int64_t>(Mp, 1) * 4, stream);
   if (M > 0) {
-    launch_bin_keys<T>(dim, xyz, M, ax, nbins, keys.as<uint32_t>(), stream);
+    launch_bin_keys<T>(dim, xyz, M, ax, nbins, cell_keys, keys.as<uint32_t>(), stream);
     stable_sort_by_bin(keys.as<uint32_t>(), M, keybits, skeys.as<uint32_t>(), perm.p, stream);
     T *const lp[3] = {loc[0].p, dim > 1 ? loc[1].p : loc[0].p, dim > 2 ? loc[2].p : loc[0].p};
     launch_sorted_local<T>(dim, xyz, perm.p, M, ax, lp, stream);
   }
   SubproblemArrays sa;
-  nsub = build_subproblems(skeys.as<uint32_t>(), M, nb, opts.gpu_maxsubprobsize, &sa, stream);
+  nsub = build_subproblems(skeys.as<uint32_t>(), M, nb, cell_keys ? (uint32_t)binvol : 1u,
+                           opts.gpu_maxsubprobsize, &sa, stream);
   sub_bin_.release();
   sub_start_.release();
   sub_count_.release();

@@ -99,24 +99,33 @@ void exclusive_scan_i32(const int *in, int *out, int64_t n, cudaStream_t s) {
 
 // ------------------------------------------------------------ bin keys ----
 namespace {
+// Sort key of a point: its bin (x fastest), times the bin volume, plus its
+// cell inside the bin (x fastest) when cell_keys is set. Sorting by this key
+// groups points by bin and, inside a bin, points that share a grid cell, so
+// the spreader can sum such runs in registers.
 template <typename T, int DIM>
 __global__ void bin_key_kernel(const T *__restrict__ x, const T *__restrict__ y,
                                const T *__restrict__ z, int M, AxisMap a0, AxisMap a1,
-                               AxisMap a2, int nb0, int nb1, uint32_t *__restrict__ keys) {
+                               AxisMap a2, int nb0, int nb1, int cell_keys,
+                               uint32_t *__restrict__ keys) {
+  const uint32_t binvol = (uint32_t)a0.bin * (DIM > 1 ? a1.bin : 1) * (DIM > 2 ? a2.bin : 1);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
     int c;
     double f;
     fold_cell((double)x[i], a0, c, f);
     uint32_t key = (uint32_t)(c / a0.bin);
+    uint32_t loc = (uint32_t)(c - (c / a0.bin) * a0.bin);
     if (DIM > 1) {
       fold_cell((double)y[i], a1, c, f);
       key += (uint32_t)nb0 * (uint32_t)(c / a1.bin);
+      loc += (uint32_t)a0.bin * (uint32_t)(c - (c / a1.bin) * a1.bin);
     }
     if (DIM > 2) {
       fold_cell((double)z[i], a2, c, f);
       key += (uint32_t)nb0 * (uint32_t)nb1 * (uint32_t)(c / a2.bin);
+      loc += (uint32_t)a0.bin * (uint32_t)a1.bin * (uint32_t)(c - (c / a2.bin) * a2.bin);
     }
-    keys[i] = key;
+    keys[i] = cell_keys ? key * binvol + loc : key;
   }
 }
 
@@ -152,18 +161,18 @@ inline unsigned grid_for(int64_t n, int threads) {
 
 template <typename T>
 void launch_bin_keys(int dim, const T *const xyz[3], int M, const AxisMap ax[3],
-                     const int nbin[3], uint32_t *keys, cudaStream_t s) {
+                     const int nbin[3], int cell_keys, uint32_t *keys, cudaStream_t s) {
   if (M <= 0) return;
   const unsigned g = grid_for(M, 256);
   if (dim == 1)
     bin_key_kernel<T, 1><<<g, 256, 0, s>>>(xyz[0], xyz[0], xyz[0], M, ax[0], ax[0], ax[0],
-                                           nbin[0], 1, keys);
+                                           nbin[0], 1, cell_keys, keys);
   else if (dim == 2)
     bin_key_kernel<T, 2><<<g, 256, 0, s>>>(xyz[0], xyz[1], xyz[1], M, ax[0], ax[1], ax[1],
-                                           nbin[0], nbin[1], keys);
+                                           nbin[0], nbin[1], cell_keys, keys);
   else
     bin_key_kernel<T, 3><<<g, 256, 0, s>>>(xyz[0], xyz[1], xyz[2], M, ax[0], ax[1], ax[2],
-                                           nbin[0], nbin[1], keys);
+                                           nbin[0], nbin[1], cell_keys, keys);
   GBN_LAUNCH_CHECK();
 }
 
@@ -185,9 +194,9 @@ void launch_sorted_local(int dim, const T *const xyz[3], const int *perm, int M,
 }
 
 template void launch_bin_keys<float>(int, const float *const[3], int, const AxisMap[3],
-                                     const int[3], uint32_t *, cudaStream_t);
+                                     const int[3], int, uint32_t *, cudaStream_t);
 template void launch_bin_keys<double>(int, const double *const[3], int, const AxisMap[3],
-                                      const int[3], uint32_t *, cudaStream_t);
+                                      const int[3], int, uint32_t *, cudaStream_t);
 template void launch_sorted_local<float>(int, const float *const[3], const int *, int,
                                          const AxisMap[3], float *const[3], cudaStream_t);
 template void launch_sorted_local<double>(int, const double *const[3], const int *, int,
@@ -310,12 +319,12 @@ void stable_sort_by_bin(uint32_t *keys_in, int M, int keybits, uint32_t *keys_ou
 
 // ----------------------------------------------------------- subproblems ----
 namespace {
-__global__ void bin_bounds_kernel(const uint32_t *__restrict__ sk, int M, int *__restrict__ bstart,
-                                  int *__restrict__ bend) {
+__global__ void bin_bounds_kernel(const uint32_t *__restrict__ sk, int M, uint32_t binvol,
+                                  int *__restrict__ bstart, int *__restrict__ bend) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
-    const uint32_t b = sk[i];
-    if (i == 0 || sk[i - 1] != b) bstart[b] = i;
-    if (i == M - 1 || sk[i + 1] != b) bend[b] = i + 1;
+    const uint32_t b = sk[i] / binvol;
+    if (i == 0 || sk[i - 1] / binvol != b) bstart[b] = i;
+    if (i == M - 1 || sk[i + 1] / binvol != b) bend[b] = i + 1;
   }
 }
 __global__ void bin_nsub_kernel(const int *__restrict__ bstart, int *__restrict__ bend_to_cnt,
@@ -342,14 +351,14 @@ __global__ void fill_subproblems_kernel(const int *__restrict__ bstart, const in
 }
 } // namespace
 
-int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, int maxsub,
-                      SubproblemArrays *out, cudaStream_t s) {
+int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, uint32_t binvol,
+                      int maxsub, SubproblemArrays *out, cudaStream_t s) {
   AsyncBuf bstart((size_t)nbins * 4, s), bcnt((size_t)nbins * 4, s), nsub((size_t)nbins * 4, s),
       substart((size_t)nbins * 4, s);
   GBN_CUDA(cudaMemsetAsync(bstart.p, 0, (size_t)nbins * 4, s));
   GBN_CUDA(cudaMemsetAsync(bcnt.p, 0, (size_t)nbins * 4, s));
   if (M > 0) {
-    bin_bounds_kernel<<<grid_for(M, 256), 256, 0, s>>>(sorted_keys, M, bstart.as<int>(),
+    bin_bounds_kernel<<<grid_for(M, 256), 256, 0, s>>>(sorted_keys, M, binvol, bstart.as<int>(),
                                                        bcnt.as<int>());
     GBN_LAUNCH_CHECK();
   }

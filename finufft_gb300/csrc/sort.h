@@ -25,10 +25,11 @@ struct AsyncBuf {
 // Exclusive prefix sum of n int32 values (out may alias nothing of in).
 void exclusive_scan_i32(const int *in, int *out, int64_t n, cudaStream_t s);
 
-// Bin key of every point: bx + nb0*(by + nb1*bz) with x fastest.
+// Sort key of every point: bin = bx + nb0*(by + nb1*bz) (x fastest); with
+// cell_keys, bin * binvol + the cell inside the bin (x fastest).
 template <typename T>
 void launch_bin_keys(int dim, const T *const xyz[3], int M, const AxisMap ax[3],
-                     const int nbin[3], uint32_t *keys, cudaStream_t s);
+                     const int nbin[3], int cell_keys, uint32_t *keys, cudaStream_t s);
 
 // Stable LSD radix sort of (key, index) pairs by the low `keybits` bits of key.
 // On return perm_out[p] is the user index of the p-th point in bin order and
@@ -41,8 +42,9 @@ void stable_sort_by_bin(uint32_t *keys_in, int M, int keybits, uint32_t *keys_ou
 struct SubproblemArrays {
   int *bin = nullptr, *start = nullptr, *count = nullptr;
 };
-int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, int maxsub,
-                      SubproblemArrays *out, cudaStream_t s);
+// binvol: keys per bin (1 for plain bin keys).
+int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, uint32_t binvol,
+                      int maxsub, SubproblemArrays *out, cudaStream_t s);
 
 // Sorted bin-local coordinates loc[d][p] in [0, bin_d], grid units.
 template <typename T>

@@ -8,10 +8,13 @@ struct SpreadConfig {
   int method;       // 1: point-driven global atomics, 2: tiled shared memory
   int threads;      // CTA size
   size_t smem;      // dynamic shared memory bytes for method 2
+  int variant = 0;  // 3D method 2: 0 shared tile + atomics, 1 exclusive warp tiles
 };
 
 // Shared-memory bytes of the tiled spread for a given tile and kernel width.
 template <typename T> size_t spread_tile_smem(int dim, int ns, const int bin[3], int threads);
+// Shared-memory bytes of the exclusive-warp 3D spread (variant 1).
+template <typename T> size_t spread_tile3w_bytes(int ns, const int bin[3]);
 
 // fw[t*nf + g] += sum_j c[t*M + j] (* pre[j] or conj(pre[j])) phi(g - x_j), t < ntr.
 // fw must be zeroed by the caller.

@@ -295,6 +295,168 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Method 2 in 3D, exclusive-warp variant: one warp per block owns its tile, so
+// the tile is updated with plain shared-memory read-modify-writes instead of
+// atomics. Points arrive sorted by (bin, cell inside the bin); the contributions
+// of a run of points that share their first support cell (frequent in
+// clustered data) are summed in registers and written to the tile once per run.
+// Lane mapping and bank-conflict-free pitches are those of spread_tile3_kernel;
+// the per-point weight products phi_y*phi_z of all NS*NS (y, z) pairs are
+// staged once per point by the lane that loaded it.
+template <typename T, int NS> struct Tile3W {
+  static constexpr int CH = t3w_chunk(NS, (int)sizeof(T)); // points staged at once
+  static constexpr int SK = CH + 1;                               // staging stride
+  static constexpr int NXB = (NS + 7) / 8;
+  static constexpr int NR = (NS * NS + 3) / 4;
+  static constexpr int NSLOT = NXB * NR;
+  static constexpr bool MERGE = NS <= 8; // register accumulators for same-cell runs
+};
+
+template <typename T, int NS>
+__global__ void __launch_bounds__(32)
+    spread_tile3w_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
+                         const cplx<T> *__restrict__ pre, int conj_pre,
+                         cplx<T> *__restrict__ fw, int64_t nf_total) {
+  using W = Tile3W<T, NS>;
+  constexpr int SK = W::SK, NR = W::NR, NXB = W::NXB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int sub = blockIdx.x, tr = blockIdx.y, lane = threadIdx.x;
+  const int b = L.sub_bin[sub];
+  const int p0 = L.sub_start[sub];
+  const int np = L.sub_count[sub];
+  const TileGeom<3> G = tile_of<T, 3, NS>(L, b);
+  const int px = tile_pitch_x(3, G.t[0]);
+  const int py = tile3_py(G.t[1], NS);
+  const int Q = px * py;
+  const int ncell = Q * G.t[2];
+  T *re = reinterpret_cast<T *>(smem_raw);
+  T *im = re + ncell;
+  T *kx = reinterpret_cast<T *>(smem_raw + tile3_bytes<T>(NS, L.bin[0], L.bin[1], L.bin[2]));
+  T *yz = kx + NS * SK;
+  T *vre = yz + 4 * NR * SK;
+  T *vim = vre + SK;
+  int *spk = reinterpret_cast<int *>(vim + SK);
+  for (int i = lane; i < 2 * ncell; i += 32) re[i] = T(0);
+  __syncwarp();
+  const int lx = lane & 7, lp = lane >> 3;
+  // tile offset of each of this lane's (x run, pair) slots
+  int off[W::MERGE ? W::NSLOT : 1];
+  bool ok[W::MERGE ? W::NSLOT : 1];
+  if constexpr (W::MERGE) {
+#pragma unroll
+    for (int xb = 0; xb < NXB; ++xb)
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const int pp = 4 * r + lp, dx = 8 * xb + lx;
+        off[xb * NR + r] = (pp / NS) * Q + (pp % NS) * px + dx;
+        ok[xb * NR + r] = dx < NS && pp < NS * NS;
+      }
+  }
+  T ar_[W::MERGE ? W::NSLOT : 1], ai_[W::MERGE ? W::NSLOT : 1];
+  int cur = -1;
+  auto flush = [&](int sp) {
+    if constexpr (W::MERGE) {
+      const int rowbase = (sp >> 20) * Q + ((sp >> 10) & 1023) * px + (sp & 1023);
+#pragma unroll
+      for (int k = 0; k < W::NSLOT; ++k)
+        if (ok[k]) {
+          re[rowbase + off[k]] += ar_[k];
+          im[rowbase + off[k]] += ai_[k];
+        }
+      __syncwarp();
+    }
+  };
+  const cplx<T> *ct = c + (int64_t)tr * L.M;
+  for (int base = 0; base < np; base += W::CH) {
+    const int i = base + lane;
+    if (lane < W::CH && i < np) {
+      const int p = p0 + i;
+      const int j = L.perm[p];
+      cplx<T> v = ct[j];
+      if (pre) v = cmul_opt<T>(v, pre[j], conj_pre);
+      T ka[NS], kb[NS], kc[NS];
+      const int sx = point_weights<T, NS>(L.loc[0][p], L.bin[0], K, ka);
+      const int sy = point_weights<T, NS>(L.loc[1][p], L.bin[1], K, kb);
+      const int sz = point_weights<T, NS>(L.loc[2][p], L.bin[2], K, kc);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) kx[a * SK + lane] = ka[a];
+#pragma unroll
+      for (int zz = 0; zz < NS; ++zz)
+#pragma unroll
+        for (int yy = 0; yy < NS; ++yy) yz[(zz * NS + yy) * SK + lane] = kb[yy] * kc[zz];
+      vre[lane] = v.x;
+      vim[lane] = v.y;
+      spk[lane] = sx | (sy << 10) | (sz << 20);
+    }
+    __syncwarp();
+    const int cnt = min(W::CH, np - base);
+    for (int q = 0; q < cnt; ++q) {
+      const int sp = spk[q];
+      const T vr = vre[q], vi = vim[q];
+      if constexpr (W::MERGE) {
+        if (sp != cur) {
+          if (cur >= 0) flush(cur);
+#pragma unroll
+          for (int k = 0; k < W::NSLOT; ++k) ar_[k] = ai_[k] = T(0);
+          cur = sp;
+        }
+#pragma unroll
+        for (int xb = 0; xb < NXB; ++xb) {
+          const T wx = kx[(8 * xb + lx) * SK + q]; // x offsets >= NS read staged yz (unused)
+          const T xr = vr * wx, xi = vi * wx;
+#pragma unroll
+          for (int r = 0; r < NR; ++r) {
+            const T w = yz[(4 * r + lp) * SK + q];
+            ar_[xb * NR + r] = fma(xr, w, ar_[xb * NR + r]);
+            ai_[xb * NR + r] = fma(xi, w, ai_[xb * NR + r]);
+          }
+        }
+      } else {
+        const int rowbase = (sp >> 20) * Q + ((sp >> 10) & 1023) * px + (sp & 1023);
+#pragma unroll
+        for (int xb = 0; xb < NXB; ++xb) {
+          const int dx = 8 * xb + lx;
+          const T wx = kx[dx * SK + q];
+          const T xr = vr * wx, xi = vi * wx;
+#pragma unroll 4
+          for (int r = 0; r < NR; ++r) {
+            const int pp = 4 * r + lp;
+            if (dx < NS && pp < NS * NS) {
+              const T w = yz[pp * SK + q];
+              const int a = rowbase + (pp / NS) * Q + (pp % NS) * px + dx;
+              re[a] += xr * w;
+              im[a] += xi * w;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
+    __syncwarp();
+  }
+  if constexpr (W::MERGE)
+    if (cur >= 0) flush(cur);
+  __syncwarp();
+  // write back row by row: 32 consecutive cells (x fastest) per step
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  const int tx = G.t[0], ty = G.t[1];
+  for (int q = lane; q < G.cells; q += 32) {
+    const int x = q % tx, rest = q / tx;
+    const int y = rest % ty, z = rest / ty;
+    const int sidx = z * Q + y * px + x;
+    cplx<T> v;
+    v.x = re[sidx];
+    v.y = im[sidx];
+    if (v.x != T(0) || v.y != T(0)) {
+      const int64_t g = wrap_idx(G.org[0] + x, L.nf[0]) +
+                        (int64_t)L.nf[0] * (wrap_idx(G.org[1] + y, L.nf[1]) +
+                                            (int64_t)L.nf[1] * wrap_idx(G.org[2] + z, L.nf[2]));
+      atomic_add_cplx_global(fwt + g, v);
+    }
+  }
+}
+
 // Method 1: point-driven spreading straight into global memory with vector
 // atomics (no tile). Points are still processed in bin order for locality.
 constexpr int GLOBAL_SPREAD_THREADS = 128;
@@ -480,6 +642,14 @@ template <typename T, int DIM> struct Dispatch {
       spread_global_kernel<T, DIM, NS><<<grid, GLOBAL_SPREAD_THREADS, 0, s>>>(L, K, c, pre, conj_pre, fw,
                                                                     nf_total);
     } else if constexpr (DIM == 3) {
+      if (cfg.variant == 1) {
+        auto kw = spread_tile3w_kernel<T, NS>;
+        GBN_CUDA(cudaFuncSetAttribute(kw, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)cfg.smem));
+        kw<<<grid, 32, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
+        GBN_LAUNCH_CHECK();
+        return;
+      }
       auto kern = spread_tile3_kernel<T, NS>;
       GBN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)cfg.smem));

@@ -25,4 +25,13 @@ __host__ __device__ constexpr size_t tile3_bytes(int ns, int bx, int by, int bz)
           15) / 16 * 16;
 }
 
+// Exclusive-warp 3D spread: points staged per step and staging bytes.
+__host__ __device__ constexpr int t3w_chunk(int ns, int tsize) {
+  return (tsize == 8 && ns > 8) ? 16 : 32;
+}
+__host__ __device__ constexpr int t3w_stage_bytes(int ns, int tsize) {
+  return ((t3w_chunk(ns, tsize) + 1) * (ns + 4 * ((ns * ns + 3) / 4) + 2) * tsize +
+          (t3w_chunk(ns, tsize) + 1) * 4 + 15) / 16 * 16;
+}
+
 } // namespace gbn

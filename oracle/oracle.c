@@ -170,32 +170,44 @@ void or_fold_cell(double x, double shift, double scale, int nf, int *cell, doubl
   *frac = r - fl;
 }
 
-/* Stable counting sort by bin (x fastest), as the CPU library's bin sort
- * (include/finufft/spread.hpp:459-584) but with the engine's fold and integer
- * bins. coords: dim arrays of doubles (the caller converts float inputs
- * exactly). Outputs perm[M] and loc[dim*M] (bin-local coordinates, rounded to
- * float when loc_is_float). Returns 0. */
+/* Stable counting sort of the points, as the CPU library's bin sort
+ * (include/finufft/spread.hpp:459-584: bins x fastest, input order kept inside
+ * a key) with the engine's fold and integer bins. The key is the bin, times the
+ * bin volume plus the cell inside the bin (x fastest) whenever
+ * bins * bin volume fits 32 bits -- the engine's device key.
+ * coords: dim arrays of doubles (float inputs converted exactly). Outputs
+ * perm[M] and loc[dim*M] (bin-local coordinates, rounded to float when
+ * loc_is_float). Returns 0. */
 int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *shift,
                 const double *scale, const int *nf, const int *bin, int32_t *perm,
                 void *loc, int loc_is_float) {
   int nb[3] = {1, 1, 1};
-  for (int d = 0; d < dim; ++d) nb[d] = (nf[d] + bin[d] - 1) / bin[d];
-  int64_t nbins = (int64_t)nb[0] * nb[1] * nb[2];
-  int64_t *cnt = (int64_t *)calloc((size_t)nbins + 1, sizeof(int64_t));
+  int bn[3] = {1, 1, 1};
+  for (int d = 0; d < dim; ++d) {
+    nb[d] = (nf[d] + bin[d] - 1) / bin[d];
+    bn[d] = bin[d];
+  }
+  const uint64_t nbins = (uint64_t)nb[0] * nb[1] * nb[2];
+  const uint64_t binvol = (uint64_t)bn[0] * bn[1] * bn[2];
+  const int cell_keys = nbins * binvol <= 0xffffffffull;
+  const uint64_t nkeys = cell_keys ? nbins * binvol : nbins;
+  int64_t *cnt = (int64_t *)calloc((size_t)nkeys + 1, sizeof(int64_t));
   uint32_t *key = (uint32_t *)malloc((size_t)(M > 0 ? M : 1) * sizeof(uint32_t));
   for (int64_t i = 0; i < M; ++i) {
-    uint32_t k = 0, stride = 1;
+    uint32_t k = 0, stride = 1, lc = 0, lstride = 1;
     for (int d = 0; d < dim; ++d) {
       int c;
       double f;
       or_fold_cell(coords[d][i], shift[d], scale[d], nf[d], &c, &f);
       k += stride * (uint32_t)(c / bin[d]);
+      lc += lstride * (uint32_t)(c - (c / bin[d]) * bin[d]);
       stride *= (uint32_t)nb[d];
+      lstride *= (uint32_t)bin[d];
     }
-    key[i] = k;
-    cnt[k + 1]++;
+    key[i] = cell_keys ? k * (uint32_t)binvol + lc : k;
+    cnt[key[i] + 1]++;
   }
-  for (int64_t b = 0; b < nbins; ++b) cnt[b + 1] += cnt[b];
+  for (uint64_t b = 0; b < nkeys; ++b) cnt[b + 1] += cnt[b];
   for (int64_t i = 0; i < M; ++i) perm[cnt[key[i]]++] = (int32_t)i;
   for (int64_t p = 0; p < M; ++p) {
     int64_t i = perm[p];

@@ -142,13 +142,16 @@ def test_bin_sort_is_stable_and_bin_ordered(oracle):
     # loc lies in [0, bin]
     for d in range(3):
         assert loc[d].min() >= 0 and loc[d].max() <= bins[d]
-    # stability: within runs of equal bins, input indices increase
+    # key = bin * binvol + cell inside the bin (x fastest); stable inside a key
     nb = [(nf[d] + bins[d] - 1) // bins[d] for d in range(3)]
     cell = []
     for d in range(3):
         r = np.mod(xs[d] / (2 * np.pi) + 0.5, 1.0) * nf[d]
-        cell.append(np.minimum(np.floor(r).astype(int), nf[d] - 1) // bins[d])
-    key = cell[0] + nb[0] * (cell[1] + nb[1] * cell[2])
+        cell.append(np.minimum(np.floor(r).astype(np.int64), nf[d] - 1))
+    b = [cell[d] // bins[d] for d in range(3)]
+    lc = [cell[d] - b[d] * bins[d] for d in range(3)]
+    key = (b[0] + nb[0] * (b[1] + nb[1] * b[2])) * (bins[0] * bins[1] * bins[2]) + \
+        lc[0] + bins[0] * (lc[1] + bins[1] * lc[2])
     ks = key[perm]
     # away from float ties the numpy key agrees with the exact fold
     assert np.mean(np.diff(ks) >= 0) > 0.999
