@@ -134,7 +134,15 @@ def run_gpu(args):
 
     import finufft_gb300 as fg
 
+    global N_MODES
     rank, world, local = dist_info()
+    if args.nmodes:
+        N_MODES = (args.nmodes,) * 3
+    plan_kw = {}
+    if args.variant >= 0:
+        plan_kw["spread_variant"] = args.variant
+    if args.planner:
+        plan_kw["planner"] = args.planner
     if world > 1:
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
@@ -149,7 +157,7 @@ def run_gpu(args):
 
     # plain GPU form: one transform, default options (reference heuristic planning)
     plain = fg.Plan(1, N_MODES, n_trans=1, eps=TOL, dtype="complex64",
-                    gpu_stream=stream.cuda_stream)
+                    gpu_stream=stream.cuda_stream, **plan_kw)
     t0 = time.perf_counter()
     plain.setpts(x, y, z)
     torch.cuda.synchronize()
@@ -333,6 +341,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4_000_000)
     ap.add_argument("--err-modes", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nmodes", type=int, default=0, help="modes per side (profiling cases)")
+    ap.add_argument("--variant", type=int, default=-1, help="3D spread variant (tuning runs)")
+    ap.add_argument("--planner", type=int, default=0, help="1: reference heuristic planning")
     ap.add_argument("--only", default="", choices=["", "plain"],
                     help="plain: time only the single-transform plan (profiling runs)")
     args = ap.parse_args()

@@ -79,16 +79,21 @@ class Plan:
         self.type, self.dim, self.n_modes, self.n_trans = nufft_type, dim, n_modes, n_trans
         self.isign, self.eps = isign, float(eps)
         self.opts = _lib.default_opts()
+        self.ext = _lib.default_ext_opts()
         names = [n for n, _ in self.opts._fields_]
+        ext_names = [n for n, _ in self.ext._fields_ if n != "reserved"]
         for k, v in kwargs.items():
-            if k not in names:
+            if k in names:
+                setattr(self.opts, k, v)
+            elif k in ext_names:
+                setattr(self.ext, k, v)
+            else:
                 raise TypeError("Invalid option '%s'" % k)
-            setattr(self.opts, k, v)
         modes = (ctypes.c_int64 * 3)(*(list(reversed(n_modes)) + [1] * (3 - dim)))
         plan = ctypes.c_void_p()
-        ier = getattr(lib, self._pfx + "_makeplan")(
+        ier = getattr(lib, self._pfx + "_makeplan_ext")(
             nufft_type, dim, modes, isign, n_trans, self.eps, ctypes.byref(plan),
-            ctypes.byref(self.opts))
+            ctypes.byref(self.opts), ctypes.byref(self.ext))
         _check("makeplan", ier)
         self._plan = plan
         self._lib = lib

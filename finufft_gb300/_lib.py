@@ -46,8 +46,15 @@ class PlanInfo(Structure):
         ("ns", c_int), ("beta", c_double), ("upsampfac", c_double),
         ("nf", c_int * 3), ("bins", c_int * 3), ("method", c_int), ("nsub", c_int),
         ("M", c_int64), ("N", c_int64), ("spread_smem", c_size_t),
-        ("horner_err", c_double), ("inner_nf", c_int * 3),
+        ("horner_err", c_double), ("inner_nf", c_int * 3), ("spread_variant", c_int),
+        ("maxsubprobsize", c_int),
     ]
+
+
+class GbnufftOpts(Structure):
+    """gbnufft_opts (include/gbnufft_ext.h)."""
+
+    _fields_ = [("planner", c_int), ("spread_variant", c_int), ("reserved", c_int * 14)]
 
 
 class FinufftOpts(Structure):
@@ -90,6 +97,10 @@ def _declare(lib):
         f.argtypes = [c_int, c_int, i64p, c_int, c_int, real, POINTER(c_void_p),
                       POINTER(CufinufftOpts)]
         f.restype = c_int
+        f = getattr(lib, pfx + "_makeplan_ext")
+        f.argtypes = [c_int, c_int, i64p, c_int, c_int, real, POINTER(c_void_p),
+                      POINTER(CufinufftOpts), POINTER(GbnufftOpts)]
+        f.restype = c_int
         f = getattr(lib, pfx + "_setpts")
         f.argtypes = [c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
                       c_void_p, c_void_p]
@@ -116,6 +127,8 @@ def _declare(lib):
     lib.finufft_default_opts.argtypes = [POINTER(FinufftOpts)]
     lib.finufft_default_opts.restype = None
     lib.gbnufft_version.restype = ctypes.c_char_p
+    lib.gbnufft_default_opts.argtypes = [POINTER(GbnufftOpts)]
+    lib.gbnufft_default_opts.restype = None
     lib.gbnufft_smem_atomic_rate.argtypes = [c_int, POINTER(c_double)]
     lib.gbnufft_smem_atomic_rate.restype = c_int
     for pfx, real in (("finufft", c_double), ("finufftf", c_float)):
@@ -134,6 +147,12 @@ def _declare(lib):
         f = getattr(lib, pfx + "_destroy")
         f.argtypes = [c_void_p]
         f.restype = c_int
+
+
+def default_ext_opts():
+    o = GbnufftOpts()
+    load().gbnufft_default_opts(ctypes.byref(o))
+    return o
 
 
 def default_opts():

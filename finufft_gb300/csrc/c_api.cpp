@@ -59,7 +59,7 @@ template <typename T> struct DevHandle {
 
 template <typename T>
 int makeplan_dev(int type, int dim, const int64_t *nmodes, int iflag, int ntr, double tol,
-                 void **out, const cufinufft_opts *opts) {
+                 void **out, const cufinufft_opts *opts, const gbnufft_opts *ext = nullptr) {
   return guarded([&] {
     if (!out) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "null plan pointer");
     if (dim < 1 || dim > 3) {
@@ -74,7 +74,7 @@ int makeplan_dev(int type, int dim, const int64_t *nmodes, int iflag, int ntr, d
     int64_t m3[3] = {1, 1, 1};
     if (type != 3)
       for (int d = 0; d < dim; ++d) m3[d] = nmodes[d];
-    h->plan.reset(new Plan<T>(type, dim, m3, iflag, ntr, tol, o));
+    h->plan.reset(new Plan<T>(type, dim, m3, iflag, ntr, tol, o, ext));
     *out = h.release();
   });
 }
@@ -137,6 +137,8 @@ template <typename T> int info_dev(void *p, gbnufft_plan_info *info) {
     info->N = P.N;
     info->spread_smem = P.spread_smem;
     info->horner_err = P.horner_err;
+    info->spread_variant = P.spread_variant_in_use();
+    info->maxsubprobsize = P.opts.gpu_maxsubprobsize;
   });
 }
 
@@ -273,6 +275,10 @@ int cufinufft_destroy(cufinufft_plan p) { return destroy_dev<double>(p); }
 int cufinufftf_destroy(cufinufftf_plan p) { return destroy_dev<float>(p); }
 
 #define GBN_EXT_DEFS(P, PLAN, T, C)                                                       \
+  int P##_makeplan_ext(int ty, int dim, const int64_t *n, int fl, int ntr, T eps, PLAN *p, \
+                       const cufinufft_opts *o, const gbnufft_opts *e) {                  \
+    return makeplan_dev<T>(ty, dim, n, fl, ntr, (double)eps, (void **)p, o, e);           \
+  }                                                                                       \
   int P##_execute_adjoint(PLAN p, C *c, C *fk) { return execute_dev<T>(p, c, fk, true); } \
   int P##_plan_info(PLAN p, gbnufft_plan_info *i) { return info_dev<T>(p, i); }           \
   int P##_stage_times(PLAN p, int en, float ms[4]) { return times_dev<T>(p, en, ms); }    \

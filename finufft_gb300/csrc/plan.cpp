@@ -7,12 +7,19 @@
 
 #include <algorithm>
 #include <cmath>
-#include <cstring>
 #include <cstdlib>
+#include <cstring>
 #include <limits>
 
 #include "planning.h"
 #include "sort.h"
+
+extern "C" void gbnufft_default_opts(gbnufft_opts *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->planner = 0;
+  o->spread_variant = -1;
+}
 
 namespace gbn {
 
@@ -38,9 +45,11 @@ int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 template <typename T>
 Plan<T>::Plan(int type_, int dim_, const int64_t *modes_in, int iflag_, int ntransf_,
-              double tol_, const cufinufft_opts &opts_)
+              double tol_, const cufinufft_opts &opts_, const gbnufft_opts *ext_)
     : type(type_), dim(dim_), ntransf(ntransf_), iflag(iflag_ >= 0 ? 1 : -1), batchsize(1),
       tol(tol_), opts(opts_) {
+  if (ext_) ext = *ext_;
+  else gbnufft_default_opts(&ext);
   if (dim < 1 || dim > 3) GBN_THROW(FINUFFT_ERR_DIM_NOTVALID, "dim");
   DeviceScope ds(opts.gpu_device_id);
   if (type < 1 || type > 3) {
@@ -61,8 +70,13 @@ Plan<T>::Plan(int type_, int dim_, const int64_t *modes_in, int iflag_, int ntra
   batchsize = opts.gpu_maxbatchsize > 0 ? opts.gpu_maxbatchsize : std::min(ntransf, 8);
   if (type == 3) batchsize = std::min(batchsize, ntransf);
   if (opts.upsampfac == 0.0) {
+    // reference rule (src/cuda/makeplan.cu:289-297): 2, or 1.25 for type 3 at
+    // tol >= 1e-9. In single precision sigma 1.25 loses digits to the wide range
+    // of 1/phihat (4e-4 error at tol 1e-6), so this engine keeps 2 there below 1e-4.
     opts.upsampfac = 2.0;
-    if (type == 3 && tol >= 1e-9) opts.upsampfac = 1.25;
+    const bool f32 = std::is_same_v<T, float>;
+    if (type == 3 && tol >= 1e-9 && (ext.planner == 1 || !f32 || tol >= 1e-4))
+      opts.upsampfac = 1.25;
   }
   const bool is_float = std::is_same_v<T, float>;
   const KernelChoice kc = choose_kernel(tol, opts.upsampfac, opts.gpu_kerevalmeth, is_float,
@@ -122,7 +136,21 @@ template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
   const int limit = max_smem_optin(opts.gpu_device_id);
   const int threads = (dim == 3 && !std::is_same_v<T, float>) ? 128 : 256;
   int def = dim == 1 ? 1024 : (dim == 2 ? 32 : 8);
-  if (dim == 3) { // largest even bin (<= 8) whose tile and staging fit in shared memory
+  if (ext.planner == 1) {
+    // the reference library's bin sizes (src/cuda/heuristics.cu:50-57,378-392):
+    // 1D 1024, 2D 40, 3D from a shared-memory budget of 50/90/100% by width
+    def = dim == 1 ? 1024 : (dim == 2 ? 40 : 0);
+    if (dim == 3) {
+      const double load = ns <= 6 ? 0.5 : (ns <= 10 ? 0.9 : 1.0);
+      auto fit = [&](double bytes) {
+        const double elems = std::floor(bytes / (2.0 * sizeof(T)));
+        return (int)std::floor(std::pow(elems, 1.0 / 3.0)) - (ns + 1);
+      };
+      def = fit(limit * load);
+      if (def < 1) def = fit(limit);
+      if (def < 1) def = 1;
+    }
+  } else if (dim == 3) { // largest even bin (<= 8) whose tile and staging fit
     while (def > 2) {
       const int b3[3] = {def, def, def};
       if (spread_tile_smem<T>(3, ns, b3, threads) <= (size_t)limit) break;
@@ -156,8 +184,10 @@ template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
   if (dim == 3 && method == 2) {
     // exclusive-warp tiles when they fit (no atomics, same-cell runs in registers)
     const size_t wsm = spread_tile3w_bytes<T>(ns, bins);
-    int variant = wsm <= (size_t)limit ? 1 : 0;
-    if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT")) variant = std::atoi(e) == 1 && wsm <= (size_t)limit ? 1 : 0;
+    int variant = (ext.planner == 1) ? 0 : (wsm <= (size_t)limit ? 1 : 0);
+    if (ext.spread_variant >= 0) variant = ext.spread_variant == 1 && wsm <= (size_t)limit ? 1 : 0;
+    if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT"))
+      variant = std::atoi(e) == 1 && wsm <= (size_t)limit ? 1 : 0;
     if (variant == 1) {
       scfg.variant = 1;
       scfg.threads = 32;
@@ -330,7 +360,7 @@ void Plan<T>::setpts(int64_t Mp, const T *x, const T *y, const T *z, int64_t Np,
   io.gpu_binsizex = io.gpu_binsizey = io.gpu_binsizez = 0;
   int64_t inner_modes[3] = {nf[0], nf[1], nf[2]};
   inner.reset();
-  inner.reset(new Plan<T>(2, dim, inner_modes, iflag, batchsize, tol, io));
+  inner.reset(new Plan<T>(2, dim, inner_modes, iflag, batchsize, tol, io, &ext));
   AxisMap iax[3];
   for (int d = 0; d < 3; ++d)
     iax[d] = AxisMap{d < dim ? t3D[d] : 0.0, d < dim ? scale[d] : 1.0, inner->nf[d],

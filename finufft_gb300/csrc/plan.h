@@ -8,6 +8,7 @@
 
 #include "common.h"
 #include "cufinufft_opts.h"
+#include "gbnufft_ext.h"
 #include "device_util.cuh"
 #include "elementwise.h"
 #include "spreadinterp.h"
@@ -51,7 +52,7 @@ struct StageTimes {
 template <typename T> class Plan {
 public:
   Plan(int type, int dim, const int64_t *nmodes, int iflag, int ntransf, double tol,
-       const cufinufft_opts &opts);
+       const cufinufft_opts &opts, const gbnufft_opts *ext = nullptr);
   ~Plan();
   void setpts(int64_t M, const T *x, const T *y, const T *z, int64_t N, const T *s,
               const T *t, const T *u);
@@ -62,6 +63,7 @@ public:
   int type, dim, ntransf, iflag, batchsize;
   double tol;
   cufinufft_opts opts;
+  gbnufft_opts ext;
   int ms[3] = {1, 1, 1};
   int nf[3] = {1, 1, 1};
   int64_t nf_total = 1, nmodes = 1;
@@ -81,6 +83,7 @@ public:
   DevArray<T> loc[3];
   DevArray<int> sub_bin_, sub_start_, sub_count_;
   PointLayout<T> layout() const;
+  int spread_variant_in_use() const { return scfg.variant; }
 
   // type 3 parameters (per dimension)
   double t3X[3] = {0, 0, 0}, t3C[3] = {0, 0, 0}, t3S[3] = {0, 0, 0}, t3D[3] = {0, 0, 0};

@@ -14,6 +14,18 @@
 extern "C" {
 #endif
 
+/* Planning options beyond cufinufft_opts (which must keep the reference's
+ * layout). Pass to cufinufft[f]_makeplan_ext; NULL means the defaults of
+ * gbnufft_default_opts. */
+typedef struct gbnufft_opts {
+  int planner;        /* 0: this engine's defaults; 1: the reference library's heuristic
+                         (cuFINUFFT 2.6 bin sizes, method and subproblem size,
+                         src/cuda/heuristics.cu:325-445) */
+  int spread_variant; /* -1 auto; 3D tiled spread: 0 shared tile with atomics,
+                         1 one warp per tile (no atomics, same-cell runs in registers) */
+  int reserved[14];
+} gbnufft_opts;
+
 typedef struct gbnufft_plan_info {
   int type, dim, ntransf, batchsize;
   int ns;              /* kernel width */
@@ -27,9 +39,18 @@ typedef struct gbnufft_plan_info {
   size_t spread_smem;  /* shared memory per spread block (method 2) */
   double horner_err;   /* max abs error of the fitted kernel pieces */
   int inner_nf[3];     /* type 3: fine grid of the inner type-2 plan */
+  int spread_variant;  /* 3D tiled spread variant in use */
+  int maxsubprobsize;  /* points per subproblem in use */
 } gbnufft_plan_info;
 
+GBNUFFT_EXPORT void gbnufft_default_opts(gbnufft_opts *o);
+
 #define GBNUFFT_EXT_DECLS(P, PLAN, T, C)                                                   \
+  /* makeplan with engine options (ext may be NULL)                                 */  \
+  GBNUFFT_EXPORT int P##_makeplan_ext(int type, int dim, const int64_t *n_modes, int iflag, \
+                                      int ntr, T eps, PLAN *plan,                        \
+                                      const cufinufft_opts *opts,                        \
+                                      const gbnufft_opts *ext);                          \
   /* Adjoint of the planned transform on device pointers (type 1 and 3: fk in,      */  \
   /* c out; type 2: c in, fk out), same semantics as finufft_execute_adjoint.       */  \
   GBNUFFT_EXPORT int P##_execute_adjoint(PLAN plan, C *d_c, C *d_fk);                    \
