@@ -313,6 +313,11 @@ template <typename T, int NS> struct Tile3W {
   static constexpr bool MERGE = NS <= 8; // register accumulators for same-cell runs
 };
 
+// periodic index for i in [-n, 2n); used when the tile is not longer than the grid
+__device__ __forceinline__ int wrap_once(int i, int n) {
+  return i < 0 ? i + n : (i >= n ? i - n : i);
+}
+
 template <typename T, int NS>
 __global__ void __launch_bounds__(32)
     spread_tile3w_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
@@ -332,12 +337,17 @@ __global__ void __launch_bounds__(32)
   const int ncell = Q * G.t[2];
   T *re = reinterpret_cast<T *>(smem_raw);
   T *im = re + ncell;
-  T *kx = reinterpret_cast<T *>(smem_raw + tile3_bytes<T>(NS, L.bin[0], L.bin[1], L.bin[2]));
+  const size_t tile_bytes = tile3_bytes<T>(NS, L.bin[0], L.bin[1], L.bin[2]);
+  T *kx = reinterpret_cast<T *>(smem_raw + tile_bytes);
   T *yz = kx + NS * SK;
   T *vre = yz + 4 * NR * SK;
   T *vim = vre + SK;
   int *spk = reinterpret_cast<int *>(vim + SK);
-  for (int i = lane; i < 2 * ncell; i += 32) re[i] = T(0);
+  {
+    uint4 *z4 = reinterpret_cast<uint4 *>(smem_raw);
+    const uint4 zero = make_uint4(0, 0, 0, 0);
+    for (int i = lane; i < (int)(tile_bytes / 16); i += 32) z4[i] = zero;
+  }
   __syncwarp();
   const int lx = lane & 7, lp = lane >> 3;
   // tile offset of each of this lane's (x run, pair) slots
@@ -391,10 +401,32 @@ __global__ void __launch_bounds__(32)
     }
     __syncwarp();
     const int cnt = min(W::CH, np - base);
-    for (int q = 0; q < cnt; ++q) {
-      const int sp = spk[q];
-      const T vr = vre[q], vi = vim[q];
-      if constexpr (W::MERGE) {
+    if constexpr (W::MERGE) {
+      // software pipeline: the staged data of point q+1 is loaded while point q
+      // is accumulated
+      int sp_n = spk[0];
+      T vr_n = vre[0], vi_n = vim[0];
+      T wx_n[NXB], w_n[NR];
+#pragma unroll
+      for (int xb = 0; xb < NXB; ++xb) wx_n[xb] = kx[(8 * xb + lx) * SK];
+#pragma unroll
+      for (int r = 0; r < NR; ++r) w_n[r] = yz[(4 * r + lp) * SK];
+      for (int q = 0; q < cnt; ++q) {
+        const int sp = sp_n;
+        const T vr = vr_n, vi = vi_n;
+        T wx[NXB], w[NR];
+#pragma unroll
+        for (int xb = 0; xb < NXB; ++xb) wx[xb] = wx_n[xb];
+#pragma unroll
+        for (int r = 0; r < NR; ++r) w[r] = w_n[r];
+        const int qn = q + 1 < cnt ? q + 1 : q;
+        sp_n = spk[qn];
+        vr_n = vre[qn];
+        vi_n = vim[qn];
+#pragma unroll
+        for (int xb = 0; xb < NXB; ++xb) wx_n[xb] = kx[(8 * xb + lx) * SK + qn];
+#pragma unroll
+        for (int r = 0; r < NR; ++r) w_n[r] = yz[(4 * r + lp) * SK + qn];
         if (sp != cur) {
           if (cur >= 0) flush(cur);
 #pragma unroll
@@ -403,30 +435,32 @@ __global__ void __launch_bounds__(32)
         }
 #pragma unroll
         for (int xb = 0; xb < NXB; ++xb) {
-          const T wx = kx[(8 * xb + lx) * SK + q]; // x offsets >= NS read staged yz (unused)
-          const T xr = vr * wx, xi = vi * wx;
+          const T xr = vr * wx[xb], xi = vi * wx[xb];
 #pragma unroll
           for (int r = 0; r < NR; ++r) {
-            const T w = yz[(4 * r + lp) * SK + q];
-            ar_[xb * NR + r] = fma(xr, w, ar_[xb * NR + r]);
-            ai_[xb * NR + r] = fma(xi, w, ai_[xb * NR + r]);
+            ar_[xb * NR + r] = fma(xr, w[r], ar_[xb * NR + r]);
+            ai_[xb * NR + r] = fma(xi, w[r], ai_[xb * NR + r]);
           }
         }
-      } else {
+      }
+    } else {
+      for (int q = 0; q < cnt; ++q) {
+        const int sp = spk[q];
+        const T vr = vre[q], vi = vim[q];
         const int rowbase = (sp >> 20) * Q + ((sp >> 10) & 1023) * px + (sp & 1023);
 #pragma unroll
         for (int xb = 0; xb < NXB; ++xb) {
           const int dx = 8 * xb + lx;
-          const T wx = kx[dx * SK + q];
+          const T wx = kx[dx * SK + q]; // x offsets >= NS read staged yz (unused)
           const T xr = vr * wx, xi = vi * wx;
 #pragma unroll 4
           for (int r = 0; r < NR; ++r) {
             const int pp = 4 * r + lp;
             if (dx < NS && pp < NS * NS) {
-              const T w = yz[pp * SK + q];
+              const T wv = yz[pp * SK + q];
               const int a = rowbase + (pp / NS) * Q + (pp % NS) * px + dx;
-              re[a] += xr * w;
-              im[a] += xi * w;
+              re[a] += xr * wv;
+              im[a] += xi * wv;
             }
           }
         }
@@ -438,21 +472,31 @@ __global__ void __launch_bounds__(32)
   if constexpr (W::MERGE)
     if (cur >= 0) flush(cur);
   __syncwarp();
-  // write back row by row: 32 consecutive cells (x fastest) per step
+  // write back: lanes cover (x, row) with rows of tx cells, 32/txp rows per step
   cplx<T> *fwt = fw + (int64_t)tr * nf_total;
-  const int tx = G.t[0], ty = G.t[1];
-  for (int q = lane; q < G.cells; q += 32) {
-    const int x = q % tx, rest = q / tx;
-    const int y = rest % ty, z = rest / ty;
-    const int sidx = z * Q + y * px + x;
-    cplx<T> v;
-    v.x = re[sidx];
-    v.y = im[sidx];
-    if (v.x != T(0) || v.y != T(0)) {
-      const int64_t g = wrap_idx(G.org[0] + x, L.nf[0]) +
-                        (int64_t)L.nf[0] * (wrap_idx(G.org[1] + y, L.nf[1]) +
-                                            (int64_t)L.nf[1] * wrap_idx(G.org[2] + z, L.nf[2]));
-      atomic_add_cplx_global(fwt + g, v);
+  const int tx = G.t[0], ty = G.t[1], tz = G.t[2];
+  const bool fits = tx <= L.nf[0] && ty <= L.nf[1] && tz <= L.nf[2] && NS <= 2 * L.nf[0] &&
+                    NS <= 2 * L.nf[1] && NS <= 2 * L.nf[2];
+  int txp = 1;
+  while (txp < tx && txp < 32) txp <<= 1;
+  const int rows_per = 32 / txp;
+  const int rows = ty * tz;
+  for (int x0 = 0; x0 < tx; x0 += txp) {
+    const int x = x0 + (lane & (txp - 1));
+    const int gx = fits ? wrap_once(G.org[0] + x, L.nf[0]) : wrap_idx(G.org[0] + x, L.nf[0]);
+    for (int r0 = lane / txp; r0 < rows; r0 += rows_per) {
+      const int y = r0 % ty, z = r0 / ty;
+      if (x < tx) {
+        const int sidx = z * Q + y * px + x;
+        cplx<T> v;
+        v.x = re[sidx];
+        v.y = im[sidx];
+        if (v.x != T(0) || v.y != T(0)) {
+          const int gy = fits ? wrap_once(G.org[1] + y, L.nf[1]) : wrap_idx(G.org[1] + y, L.nf[1]);
+          const int gz = fits ? wrap_once(G.org[2] + z, L.nf[2]) : wrap_idx(G.org[2] + z, L.nf[2]);
+          atomic_add_cplx_global(fwt + gx + (int64_t)L.nf[0] * (gy + (int64_t)L.nf[1] * gz), v);
+        }
+      }
     }
   }
 }
