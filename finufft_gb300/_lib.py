@@ -127,6 +127,10 @@ def _declare(lib):
     lib.finufft_default_opts.argtypes = [POINTER(FinufftOpts)]
     lib.finufft_default_opts.restype = None
     lib.gbnufft_version.restype = ctypes.c_char_p
+    lib.cufinufftf_spread_noalloc.argtypes = [c_int, POINTER(c_int64), c_int64, c_void_p,
+                                              c_void_p, c_void_p, c_void_p, c_void_p, c_float,
+                                              c_void_p]
+    lib.cufinufftf_spread_noalloc.restype = c_int
     lib.gbnufft_default_opts.argtypes = [POINTER(GbnufftOpts)]
     lib.gbnufft_default_opts.restype = None
     lib.gbnufft_smem_atomic_rate.argtypes = [c_int, POINTER(c_double)]

@@ -28,6 +28,7 @@ CU_SOURCES = [
     "spreadinterp_1d.cu",
     "spreadinterp_2d.cu",
     "spreadinterp_3d.cu",
+    "noalloc.cu",
 ]
 CPP_SOURCES = ["planning.cpp", "plan.cpp", "c_api.cpp", "host_api.cpp"]
 

@@ -75,32 +75,13 @@ Plan<T>::Plan(int type_, int dim_, const int64_t *modes_in, int iflag_, int ntra
     // of 1/phihat (4e-4 error at tol 1e-6), so this engine keeps 2 there below 1e-4.
     opts.upsampfac = 2.0;
     const bool f32 = std::is_same_v<T, float>;
-    if (type == 3 && tol >= 1e-9 && (ext.planner == 1 || !f32 || tol >= 1e-4))
+    if (type == 3 && tol >= 1e-9 && (ext.planner == 1 || !f32 || (float)tol >= 1e-4f))
       opts.upsampfac = 1.25;
   }
   const bool is_float = std::is_same_v<T, float>;
   const KernelChoice kc = choose_kernel(tol, opts.upsampfac, opts.gpu_kerevalmeth, is_float,
                                         opts.gpu_spreadinterponly, opts.debug);
-  std::memset(&K, 0, sizeof(K));
-  K.ns = kc.ns;
-  K.beta = (T)kc.beta;
-  K.es_c = (T)(4.0 / (double(kc.ns) * kc.ns));
-  K.use_horner = opts.gpu_kerevalmeth == 1 ? 1 : 0;
-  {
-    // Horner pieces are fitted for any sigma; the reference only carries tables
-    // for sigma 2 and 1.25, which the option check above already enforces.
-    std::vector<double> coef;
-    const double target = std::max(1e-2 * tol, is_float ? 2e-7 : 4e-15);
-    const int H = horner_len(kc.ns);
-    const int ncoef = horner_fit(kc.ns, kc.beta, target, H, coef, &horner_err);
-    K.ncoef = H;
-    for (int k = 0; k < H; ++k)
-      for (int j = 0; j < kc.ns; ++j) {
-        const int src = k - (H - ncoef); // zero-pad the high-degree end
-        K.coef[k][j] = src >= 0 ? (T)coef[(size_t)src * MAX_NS + j] : T(0);
-      }
-    if (ncoef > H) K.use_horner = 0; // (cannot happen: fit is capped at MAX_HCOEF)
-  }
+  horner_err = build_kernel_shape<T>(kc.ns, kc.beta, opts.gpu_kerevalmeth == 1, tol, &K);
   if (type != 3) {
     for (int d = 0; d < dim; ++d)
       nf[d] = opts.gpu_spreadinterponly ? ms[d]
@@ -130,9 +111,11 @@ template <typename T> Plan<T>::~Plan() {
   }
 }
 
-template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
+template <typename T>
+SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts &opts,
+                         const gbnufft_opts &ext, bool user_method) {
+  SpreadSetup S;
   // bins: the user's values, else this engine's defaults per dimension
-  const int ns = K.ns;
   const int limit = max_smem_optin(opts.gpu_device_id);
   const int threads = (dim == 3 && !std::is_same_v<T, float>) ? 128 : 256;
   int def = dim == 1 ? 1024 : (dim == 2 ? 32 : 8);
@@ -157,6 +140,7 @@ template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
       def -= 2;
     }
   }
+  int *bins = S.bins, *nbins = S.nbins;
   bins[0] = opts.gpu_binsizex > 0 ? opts.gpu_binsizex : def;
   bins[1] = dim > 1 ? (opts.gpu_binsizey > 0 ? opts.gpu_binsizey : def) : 1;
   bins[2] = dim > 2 ? (opts.gpu_binsizez > 0 ? opts.gpu_binsizez : def) : 1;
@@ -167,21 +151,21 @@ template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
   if (dim == 3 && (bins[0] > 1000 || bins[1] > 1000 || bins[2] > 1000))
     GBN_THROW(FINUFFT_ERR_BINSIZE_NOTVALID, "3D bins must be < 1000");
   if (opts.gpu_maxsubprobsize < 1) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "maxsubprobsize");
-  method = opts.gpu_method == 0 ? 2 : (opts.gpu_method == 1 ? 1 : 2);
-  spread_smem = spread_tile_smem<T>(dim, ns, bins, threads);
-  if (method == 2 && spread_smem > (size_t)limit) {
+  S.method = opts.gpu_method == 0 ? 2 : (opts.gpu_method == 1 ? 1 : 2);
+  S.smem = spread_tile_smem<T>(dim, ns, bins, threads);
+  if (S.method == 2 && S.smem > (size_t)limit) {
     if (user_method) {
-      fprintf(stderr, "[gbnufft] tile needs %zu bytes of shared memory, %d available\n",
-              spread_smem, limit);
+      fprintf(stderr, "[gbnufft] tile needs %zu bytes of shared memory, %d available\n", S.smem,
+              limit);
       GBN_THROW(FINUFFT_ERR_INSUFFICIENT_SHMEM, "tile too large");
     }
-    method = 1;
+    S.method = 1;
   }
-  scfg.method = method;
-  scfg.threads = threads;
-  scfg.smem = method == 2 ? spread_smem : 0;
-  scfg.variant = 0;
-  if (dim == 3 && method == 2) {
+  S.cfg.method = S.method;
+  S.cfg.threads = threads;
+  S.cfg.smem = S.method == 2 ? S.smem : 0;
+  S.cfg.variant = 0;
+  if (dim == 3 && S.method == 2) {
     // exclusive-warp tiles when they fit (no atomics, same-cell runs in registers)
     const size_t wsm = spread_tile3w_bytes<T>(ns, bins);
     int variant = (ext.planner == 1) ? 0 : (wsm <= (size_t)limit ? 1 : 0);
@@ -189,12 +173,28 @@ template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
     if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT"))
       variant = std::atoi(e) == 1 && wsm <= (size_t)limit ? 1 : 0;
     if (variant == 1) {
-      scfg.variant = 1;
-      scfg.threads = 32;
-      scfg.smem = wsm;
-      spread_smem = wsm;
+      S.cfg.variant = 1;
+      S.cfg.threads = 32;
+      S.cfg.smem = wsm;
+      S.smem = wsm;
     }
   }
+  return S;
+}
+template SpreadSetup spread_setup<float>(int, int, const int[3], const cufinufft_opts &,
+                                         const gbnufft_opts &, bool);
+template SpreadSetup spread_setup<double>(int, int, const int[3], const cufinufft_opts &,
+                                          const gbnufft_opts &, bool);
+
+template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
+  const SpreadSetup S = spread_setup<T>(dim, K.ns, nf, opts, ext, user_method);
+  for (int d = 0; d < 3; ++d) {
+    bins[d] = S.bins[d];
+    nbins[d] = S.nbins[d];
+  }
+  method = S.method;
+  spread_smem = S.smem;
+  scfg = S.cfg;
 }
 
 template <typename T> void Plan<T>::make_fft() {

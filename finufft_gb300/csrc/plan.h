@@ -49,6 +49,18 @@ struct StageTimes {
   float spread_or_interp_ms = 0, fft_ms = 0, deconv_ms = 0, total_ms = 0;
 };
 
+// Bins, method and launch configuration of the spreader for a grid.
+struct SpreadSetup {
+  int bins[3] = {1, 1, 1};
+  int nbins[3] = {1, 1, 1};
+  int method = 2;
+  size_t smem = 0;
+  SpreadConfig cfg{2, 256, 0};
+};
+template <typename T>
+SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts &opts,
+                         const gbnufft_opts &ext, bool user_method);
+
 template <typename T> class Plan {
 public:
   Plan(int type, int dim, const int64_t *nmodes, int iflag, int ntransf, double tol,

@@ -10,6 +10,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <limits>
 
 #include "common.h"
@@ -273,5 +274,31 @@ int kernel_ft_nodes(int ns, double beta, double nodes_per_halfwidth, double *z, 
   }
   return q;
 }
+
+template <typename T>
+double build_kernel_shape(int ns, double beta, int use_horner, double tol, KernelShape<T> *K) {
+  std::memset(K, 0, sizeof(*K));
+  K->ns = ns;
+  K->beta = (T)beta;
+  K->es_c = (T)(4.0 / (double(ns) * ns));
+  K->use_horner = use_horner ? 1 : 0;
+  // pieces are fitted for any sigma; the reference only carries tables for
+  // sigma 2 and 1.25, which the option check already enforces
+  std::vector<double> coef;
+  double err = 0;
+  const bool is_float = std::is_same_v<T, float>;
+  const double target = std::max(1e-2 * tol, is_float ? 2e-7 : 4e-15);
+  const int H = horner_len(ns);
+  const int ncoef = horner_fit(ns, beta, target, H, coef, &err);
+  K->ncoef = H;
+  for (int k = 0; k < H; ++k)
+    for (int j = 0; j < ns; ++j) {
+      const int src = k - (H - ncoef); // zero-pad the high-degree end
+      K->coef[k][j] = src >= 0 ? (T)coef[(size_t)src * MAX_NS + j] : T(0);
+    }
+  return err;
+}
+template double build_kernel_shape<float>(int, double, int, double, KernelShape<float> *);
+template double build_kernel_shape<double>(int, double, int, double, KernelShape<double> *);
 
 } // namespace gbn

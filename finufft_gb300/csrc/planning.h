@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <vector>
 
+#include "common.h"
+
 namespace gbn {
 
 // Smallest even 2,3,5-smooth integer >= n (FINUFFT's next235(n, 2)).
@@ -43,5 +45,10 @@ int horner_fit(int ns, double beta, double target_err, int maxcoef, std::vector<
 //   phihat(k) = sum_n f[n] * 2 cos(k z[n]),  z in grid units.
 // q = number of nodes used.
 int kernel_ft_nodes(int ns, double beta, double nodes_per_halfwidth, double *z, double *f);
+
+// Fill the kernel description passed to spread/interp kernels: ES shape, and
+// Horner pieces fitted to max(tol/100, a few ulps). Returns the fit's max error.
+template <typename T>
+double build_kernel_shape(int ns, double beta, int use_horner, double tol, KernelShape<T> *K);
 
 } // namespace gbn

@@ -81,7 +81,7 @@ __global__ void scan_chunks(const int *__restrict__ in, int64_t n,
 }
 } // namespace
 
-void exclusive_scan_i32(const int *in, int *out, int64_t n, cudaStream_t s) {
+void exclusive_scan_i32(const int *in, int *out, int64_t n, cudaStream_t s, Arena *arena) {
   if (n <= 0) return;
   const int64_t nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
   if (nb == 1) {
@@ -89,10 +89,10 @@ void exclusive_scan_i32(const int *in, int *out, int64_t n, cudaStream_t s) {
     GBN_LAUNCH_CHECK();
     return;
   }
-  AsyncBuf sums(nb * sizeof(int), s), offs(nb * sizeof(int), s);
+  AsyncBuf sums(nb * sizeof(int), s, arena), offs(nb * sizeof(int), s, arena);
   scan_block_sums<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, sums.as<int>());
   GBN_LAUNCH_CHECK();
-  exclusive_scan_i32(sums.as<int>(), offs.as<int>(), nb, s);
+  exclusive_scan_i32(sums.as<int>(), offs.as<int>(), nb, s, arena);
   scan_chunks<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, offs.as<int>(), out);
   GBN_LAUNCH_CHECK();
 }
@@ -285,7 +285,7 @@ __global__ void iota_kernel(int *v, int M) {
 } // namespace
 
 void stable_sort_by_bin(uint32_t *keys_in, int M, int keybits, uint32_t *keys_out,
-                        int *perm_out, cudaStream_t s) {
+                        int *perm_out, cudaStream_t s, Arena *arena) {
   if (M <= 0) return;
   const int passes = (keybits + 7) / 8;
   if (passes == 0) { // single bin: identity permutation
@@ -295,9 +295,9 @@ void stable_sort_by_bin(uint32_t *keys_in, int M, int keybits, uint32_t *keys_ou
     return;
   }
   const int ntiles = (int)(((int64_t)M + RS_TILE - 1) / RS_TILE);
-  AsyncBuf hist((size_t)256 * ntiles * sizeof(int), s);
-  AsyncBuf offs((size_t)256 * ntiles * sizeof(int), s);
-  AsyncBuf ktmp((size_t)M * 4, s), vtmp((size_t)M * 4, s);
+  AsyncBuf hist((size_t)256 * ntiles * sizeof(int), s, arena);
+  AsyncBuf offs((size_t)256 * ntiles * sizeof(int), s, arena);
+  AsyncBuf ktmp((size_t)M * 4, s, arena), vtmp((size_t)M * 4, s, arena);
   // ping-pong so the last pass lands in (keys_out, perm_out)
   const uint32_t *ks = keys_in;
   const int *vs = nullptr; // pass 0 uses the identity as values
@@ -308,7 +308,7 @@ void stable_sort_by_bin(uint32_t *keys_in, int M, int keybits, uint32_t *keys_ou
     const int shift = 8 * p;
     radix_hist_kernel<<<ntiles, RS_THREADS, 0, s>>>(ks, M, shift, ntiles, hist.as<int>());
     GBN_LAUNCH_CHECK();
-    exclusive_scan_i32(hist.as<int>(), offs.as<int>(), (int64_t)256 * ntiles, s);
+    exclusive_scan_i32(hist.as<int>(), offs.as<int>(), (int64_t)256 * ntiles, s, arena);
     radix_scatter_kernel<<<ntiles, RS_THREADS, 0, s>>>(ks, vs, kd, vd, M, shift, ntiles,
                                                        offs.as<int>());
     GBN_LAUNCH_CHECK();
@@ -352,9 +352,9 @@ __global__ void fill_subproblems_kernel(const int *__restrict__ bstart, const in
 } // namespace
 
 int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, uint32_t binvol,
-                      int maxsub, SubproblemArrays *out, cudaStream_t s) {
-  AsyncBuf bstart((size_t)nbins * 4, s), bcnt((size_t)nbins * 4, s), nsub((size_t)nbins * 4, s),
-      substart((size_t)nbins * 4, s);
+                      int maxsub, SubproblemArrays *out, cudaStream_t s, Arena *arena) {
+  AsyncBuf bstart((size_t)nbins * 4, s, arena), bcnt((size_t)nbins * 4, s, arena),
+      nsub((size_t)nbins * 4, s, arena), substart((size_t)nbins * 4, s, arena);
   GBN_CUDA(cudaMemsetAsync(bstart.p, 0, (size_t)nbins * 4, s));
   GBN_CUDA(cudaMemsetAsync(bcnt.p, 0, (size_t)nbins * 4, s));
   if (M > 0) {
@@ -365,20 +365,26 @@ int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, uint32_t bi
   bin_nsub_kernel<<<grid_for(nbins, 256), 256, 0, s>>>(bstart.as<int>(), bcnt.as<int>(),
                                                        nsub.as<int>(), nbins, maxsub);
   GBN_LAUNCH_CHECK();
-  exclusive_scan_i32(nsub.as<int>(), substart.as<int>(), nbins, s);
+  exclusive_scan_i32(nsub.as<int>(), substart.as<int>(), nbins, s, arena);
   int last[2] = {0, 0};
   GBN_CUDA(cudaMemcpyAsync(&last[0], substart.as<int>() + nbins - 1, 4, cudaMemcpyDeviceToHost, s));
   GBN_CUDA(cudaMemcpyAsync(&last[1], nsub.as<int>() + nbins - 1, 4, cudaMemcpyDeviceToHost, s));
   GBN_CUDA(cudaStreamSynchronize(s));
   const int total = last[0] + last[1];
-  if (out->bin) cudaFree(out->bin);
-  if (out->start) cudaFree(out->start);
-  if (out->count) cudaFree(out->count);
-  out->bin = out->start = out->count = nullptr;
   const size_t nalloc = (size_t)(total > 0 ? total : 1) * 4;
-  GBN_CUDA(cudaMalloc(&out->bin, nalloc));
-  GBN_CUDA(cudaMalloc(&out->start, nalloc));
-  GBN_CUDA(cudaMalloc(&out->count, nalloc));
+  if (arena) {
+    out->bin = (int *)arena->take(nalloc);
+    out->start = (int *)arena->take(nalloc);
+    out->count = (int *)arena->take(nalloc);
+  } else {
+    if (out->bin) cudaFree(out->bin);
+    if (out->start) cudaFree(out->start);
+    if (out->count) cudaFree(out->count);
+    out->bin = out->start = out->count = nullptr;
+    GBN_CUDA(cudaMalloc(&out->bin, nalloc));
+    GBN_CUDA(cudaMalloc(&out->start, nalloc));
+    GBN_CUDA(cudaMalloc(&out->count, nalloc));
+  }
   fill_subproblems_kernel<<<grid_for(nbins, 256), 256, 0, s>>>(
       bstart.as<int>(), bcnt.as<int>(), nsub.as<int>(), substart.as<int>(), nbins, maxsub,
       out->bin, out->start, out->count);

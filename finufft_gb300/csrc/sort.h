@@ -6,16 +6,37 @@
 
 namespace gbn {
 
-// Stream-ordered device scratch buffer (cudaMallocAsync / cudaFreeAsync).
+// A caller-provided block of device memory handed out front to back
+// (256-byte aligned pieces, never freed individually).
+struct Arena {
+  unsigned char *base = nullptr;
+  size_t cap = 0, used = 0;
+  void *take(size_t bytes) {
+    const size_t at = (used + 255) / 256 * 256;
+    if (at + bytes > cap) GBN_THROW(FINUFFT_ERR_ALLOC, "scratch arena exhausted");
+    used = at + bytes;
+    return base + at;
+  }
+};
+
+// Device scratch: from an Arena when one is given, else stream-ordered
+// cudaMallocAsync / cudaFreeAsync.
 struct AsyncBuf {
   void *p = nullptr;
   cudaStream_t s = nullptr;
+  bool owned = false;
   AsyncBuf() = default;
-  AsyncBuf(size_t bytes, cudaStream_t st) : s(st) {
-    if (bytes) GBN_CUDA(cudaMallocAsync(&p, bytes, st));
+  AsyncBuf(size_t bytes, cudaStream_t st, Arena *arena = nullptr) : s(st) {
+    if (!bytes) return;
+    if (arena) {
+      p = arena->take(bytes);
+    } else {
+      GBN_CUDA(cudaMallocAsync(&p, bytes, st));
+      owned = true;
+    }
   }
   ~AsyncBuf() {
-    if (p) cudaFreeAsync(p, s);
+    if (p && owned) cudaFreeAsync(p, s);
   }
   AsyncBuf(const AsyncBuf &) = delete;
   AsyncBuf &operator=(const AsyncBuf &) = delete;
@@ -23,7 +44,8 @@ struct AsyncBuf {
 };
 
 // Exclusive prefix sum of n int32 values (out may alias nothing of in).
-void exclusive_scan_i32(const int *in, int *out, int64_t n, cudaStream_t s);
+void exclusive_scan_i32(const int *in, int *out, int64_t n, cudaStream_t s,
+                        Arena *arena = nullptr);
 
 // Sort key of every point: bin = bx + nb0*(by + nb1*bz) (x fastest); with
 // cell_keys, bin * binvol + the cell inside the bin (x fastest).
@@ -35,16 +57,19 @@ void launch_bin_keys(int dim, const T *const xyz[3], int M, const AxisMap ax[3],
 // On return perm_out[p] is the user index of the p-th point in bin order and
 // keys_out[p] its bin. keys_in is clobbered.
 void stable_sort_by_bin(uint32_t *keys_in, int M, int keybits, uint32_t *keys_out,
-                        int *perm_out, cudaStream_t s);
+                        int *perm_out, cudaStream_t s, Arena *arena = nullptr);
 
 // Per-bin [start, count) of the sorted keys and subproblem decomposition.
 // Returns the number of subproblems (one device->host copy, stream sync).
 struct SubproblemArrays {
   int *bin = nullptr, *start = nullptr, *count = nullptr;
 };
-// binvol: keys per bin (1 for plain bin keys).
+// binvol: keys per bin (1 for plain bin keys). With an arena the three output
+// arrays are carved from it (nothing to free); otherwise they are cudaMalloc'd
+// and the previous contents of *out are cudaFree'd.
 int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, uint32_t binvol,
-                      int maxsub, SubproblemArrays *out, cudaStream_t s);
+                      int maxsub, SubproblemArrays *out, cudaStream_t s,
+                      Arena *arena = nullptr);
 
 // Sorted bin-local coordinates loc[d][p] in [0, bin_d], grid units.
 template <typename T>

@@ -73,6 +73,24 @@ GBNUFFT_EXT_DECLS(cufinufftf, cufinufftf_plan, float, cuFloatComplex)
  * (lane operations per second), the peak the spreading kernels are held to. */
 GBNUFFT_EXPORT int gbnufft_smem_atomic_rate(int device, double *rate);
 
+/* Spread-only type 1 without device allocation (no counterpart in the
+ * reference): grid[g] = sum_j c[j] phi(g - x_j) on the periodic grid of
+ * n_grid[0..dim) cells (x fastest), the same result as a cufinufftf plan of
+ * type 1 with gpu_spreadinterponly = 1 and default options. For callers that
+ * may not allocate device memory (a foreign allocator owns the GPU, or all
+ * memory is reserved at start-up): every intermediate lives in a fixed 32 MiB
+ * scratch array compiled into the library, which each GPU that loads the
+ * library holds until exit. Limits: M <= 2^19 points, at most 2^24 grid cells;
+ * larger inputs return FINUFFT_ERR_MAXNALLOC. The first call on a device looks
+ * up the scratch address on that device; make that first call before any
+ * stream capture. Calls share the scratch, so calls that overlap on the GPU
+ * race: order them on one stream. Blocks the host until the bin sort is done,
+ * as setpts does. All pointers are device pointers; stream may be NULL. */
+GBNUFFT_EXPORT int cufinufftf_spread_noalloc(int dim, const int64_t *n_grid, int64_t M,
+                                             const float *d_x, const float *d_y,
+                                             const float *d_z, const cuFloatComplex *d_c,
+                                             cuFloatComplex *d_grid, float eps, void *stream);
+
 /* Library build identification string. */
 GBNUFFT_EXPORT const char *gbnufft_version(void);
 

@@ -332,7 +332,10 @@ def nufft_es(nufft_type, xs, data, isign, tol, n_modes=None, ss=None, sigma=None
     reversed(n_modes) (type 2). Type 3: ss = target coordinates."""
     dim = len(xs)
     if sigma is None:
-        sigma = 1.25 if (nufft_type == 3 and tol >= 1e-9) else 2.0
+        # the engine's rule: 1.25 for type 3 at tol >= 1e-9, but in single
+        # precision only at tol >= 1e-4 (compared in single precision)
+        ok = np.float32(tol) >= np.float32(1e-4) if is_float else tol >= 1e-9
+        sigma = 1.25 if (nufft_type == 3 and tol >= 1e-9 and ok) else 2.0
     ns, beta = gpu_kernel(tol, sigma, 1, is_float)
     fun = lambda x: es_kernel(x, ns, beta)
     if nufft_type in (1, 2):
