@@ -166,14 +166,18 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
   S.cfg.smem = S.method == 2 ? S.smem : 0;
   S.cfg.variant = 0;
   if (dim == 3 && S.method == 2) {
-    // exclusive-warp tiles when they fit (no atomics, same-cell runs in registers)
+    // 3D tiled variants: 0 shared tile + per-point atomics, 1 exclusive-warp tiles,
+    // 2 shared tile + per-run (warp-aggregated) atomics; default 2
     const size_t wsm = spread_tile3w_bytes<T>(ns, bins);
-    int variant = (ext.planner == 1) ? 0 : (wsm <= (size_t)limit ? 1 : 0);
-    if (ext.spread_variant >= 0) variant = ext.spread_variant == 1 && wsm <= (size_t)limit ? 1 : 0;
-    if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT"))
-      variant = std::atoi(e) == 1 && wsm <= (size_t)limit ? 1 : 0;
+    // per-run register accumulators cost 2*ceil(ns/8)*ceil(ns^2/4) registers, so
+    // the warp-aggregated variant is used for ns <= 8 only
+    int variant = ext.planner == 1 ? 0 : (ns <= 8 ? 2 : 0);
+    if (ext.spread_variant >= 0) variant = ext.spread_variant;
+    if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT")) variant = std::atoi(e);
+    if (variant == 1 && wsm > (size_t)limit) variant = 2;
+    if (variant < 0 || variant > 2 || (variant == 2 && ns > 8)) variant = 0;
+    S.cfg.variant = variant;
     if (variant == 1) {
-      S.cfg.variant = 1;
       S.cfg.threads = 32;
       S.cfg.smem = wsm;
       S.smem = wsm;

@@ -48,6 +48,11 @@ __device__ __forceinline__ int wrap_idx(int i, int n) {
   return i < 0 ? i + n : i;
 }
 
+// periodic index for i in [-n, 2n); used when the tile is not longer than the grid
+__device__ __forceinline__ int wrap_once(int i, int n) {
+  return i < 0 ? i + n : (i >= n ? i - n : i);
+}
+
 // first support cell (tile coordinates) and kernel weights of one point
 template <typename T, int NS>
 __device__ __forceinline__ int point_weights(T l, int binsz, const KernelShape<T> &K, T *ker) {
@@ -296,6 +301,163 @@ __global__ void __launch_bounds__(256)
 }
 
 // ---------------------------------------------------------------------------
+// Method 2 in 3D, warp-aggregated variant: the tile is shared by the block's
+// warps (atomics, as in spread_tile3_kernel), but each warp takes a contiguous
+// range of the (bin, cell)-sorted points and sums the contributions of a run
+// of points with the same first support cell in registers, issuing the tile
+// atomics once per run instead of once per point. Staging and lane mapping
+// are those of spread_tile3_kernel.
+template <typename T, int NS>
+__global__ void __launch_bounds__(256)
+    spread_tile3m_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
+                         const cplx<T> *__restrict__ pre, int conj_pre,
+                         cplx<T> *__restrict__ fw, int64_t nf_total) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int SK = STAGE_STRIDE;
+  constexpr int NXB = (NS + 7) / 8;
+  constexpr int NR = (NS * NS + 3) / 4;
+  constexpr int NSLOT = NXB * NR;
+  const int sub = blockIdx.x;
+  const int tr = blockIdx.y;
+  const int b = L.sub_bin[sub];
+  const int p0 = L.sub_start[sub];
+  const int np = L.sub_count[sub];
+  const TileGeom<3> G = tile_of<T, 3, NS>(L, b);
+  const int px = tile_pitch_x(3, G.t[0]);
+  const int py = tile3_py(G.t[1], NS);
+  const int Q = px * py;
+  const size_t tile_bytes = tile3_bytes<T>(NS, L.bin[0], L.bin[1], L.bin[2]);
+  T *re = reinterpret_cast<T *>(smem_raw);
+  T *im = re + Q * G.t[2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  unsigned char *stage = smem_raw + tile_bytes + (size_t)warp * stage_bytes_per_warp<T>(NS);
+  T *kx = reinterpret_cast<T *>(stage);
+  T *ky = kx + NS * SK;
+  T *kz = ky + NS * SK;
+  T *vre = kz + NS * SK;
+  T *vim = vre + SK;
+  int *spk = reinterpret_cast<int *>(vim + SK);
+  {
+    uint4 *z4 = reinterpret_cast<uint4 *>(smem_raw);
+    const uint4 zero = make_uint4(0, 0, 0, 0);
+    for (int i = threadIdx.x; i < (int)(tile_bytes / 16); i += blockDim.x) z4[i] = zero;
+  }
+  __syncthreads();
+  const int lx = lane & 7, lp = lane >> 3;
+  int off[NSLOT], iy[NSLOT], iz[NSLOT];
+  bool ok[NSLOT];
+#pragma unroll
+  for (int xb = 0; xb < NXB; ++xb)
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      const int pp = 4 * r + lp, dx = 8 * xb + lx, k = xb * NR + r;
+      const int dy = pp % NS, dz = pp / NS;
+      ok[k] = dx < NS && pp < NS * NS;
+      iy[k] = (ok[k] ? dy : 0) * SK;
+      iz[k] = (ok[k] ? dz : 0) * SK;
+      off[k] = dz * Q + dy * px + dx;
+    }
+  T ar[NSLOT], ai[NSLOT];
+  int cur = -1;
+  // contiguous share of the subproblem's points for this warp (keeps runs whole)
+  const int per = (np + nwarp - 1) / nwarp;
+  const int w0 = min(np, warp * per), w1 = min(np, w0 + per);
+  const cplx<T> *ct = c + (int64_t)tr * L.M;
+  for (int base = w0; base < w1; base += 32) {
+    const int i = base + lane;
+    if (i < w1) {
+      const int p = p0 + i;
+      const int j = L.perm[p];
+      cplx<T> v = ct[j];
+      if (pre) v = cmul_opt<T>(v, pre[j], conj_pre);
+      T kk[NS];
+      const int sx = point_weights<T, NS>(L.loc[0][p], L.bin[0], K, kk);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) kx[a * SK + lane] = kk[a];
+      const int sy = point_weights<T, NS>(L.loc[1][p], L.bin[1], K, kk);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) ky[a * SK + lane] = kk[a];
+      const int sz = point_weights<T, NS>(L.loc[2][p], L.bin[2], K, kk);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) kz[a * SK + lane] = kk[a];
+      vre[lane] = v.x;
+      vim[lane] = v.y;
+      spk[lane] = sx | (sy << 10) | (sz << 20);
+    }
+    __syncwarp();
+    const int cnt = min(32, w1 - base);
+    for (int q = 0; q < cnt; ++q) {
+      const int sp = spk[q];
+      if (sp != cur) {
+        if (cur >= 0) {
+          const int rb = (cur >> 20) * Q + ((cur >> 10) & 1023) * px + (cur & 1023);
+#pragma unroll
+          for (int k = 0; k < NSLOT; ++k)
+            if (ok[k]) {
+              atomicAdd(re + rb + off[k], ar[k]);
+              atomicAdd(im + rb + off[k], ai[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NSLOT; ++k) ar[k] = ai[k] = T(0);
+        cur = sp;
+      }
+      const T vr = vre[q], vi = vim[q];
+#pragma unroll
+      for (int xb = 0; xb < NXB; ++xb) {
+        const T wx = kx[(8 * xb + lx) * SK + q]; // x offsets >= NS read staged y weights
+        const T xr = vr * wx, xi = vi * wx;
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+          const int k = xb * NR + r;
+          const T w = ky[iy[k] + q] * kz[iz[k] + q];
+          ar[k] = fma(xr, w, ar[k]);
+          ai[k] = fma(xi, w, ai[k]);
+        }
+      }
+    }
+    __syncwarp();
+  }
+  if (cur >= 0) {
+    const int rb = (cur >> 20) * Q + ((cur >> 10) & 1023) * px + (cur & 1023);
+#pragma unroll
+    for (int k = 0; k < NSLOT; ++k)
+      if (ok[k]) {
+        atomicAdd(re + rb + off[k], ar[k]);
+        atomicAdd(im + rb + off[k], ai[k]);
+      }
+  }
+  __syncthreads();
+  // write back: lanes cover (x, row) pairs, rows of tx cells
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  const int tx = G.t[0], ty = G.t[1], tz = G.t[2];
+  const bool fits = tx <= L.nf[0] && ty <= L.nf[1] && tz <= L.nf[2] && NS <= 2 * L.nf[0] &&
+                    NS <= 2 * L.nf[1] && NS <= 2 * L.nf[2];
+  int txp = 1;
+  while (txp < tx && txp < 32) txp <<= 1;
+  const int rows_per = blockDim.x / txp;
+  const int rows = ty * tz;
+  for (int x0 = 0; x0 < tx; x0 += txp) {
+    const int x = x0 + (threadIdx.x & (txp - 1));
+    const int gx = fits ? wrap_once(G.org[0] + x, L.nf[0]) : wrap_idx(G.org[0] + x, L.nf[0]);
+    for (int r0 = threadIdx.x / txp; r0 < rows; r0 += rows_per) {
+      const int y = r0 % ty, z = r0 / ty;
+      if (x < tx) {
+        const int sidx = z * Q + y * px + x;
+        cplx<T> v;
+        v.x = re[sidx];
+        v.y = im[sidx];
+        if (v.x != T(0) || v.y != T(0)) {
+          const int gy = fits ? wrap_once(G.org[1] + y, L.nf[1]) : wrap_idx(G.org[1] + y, L.nf[1]);
+          const int gz = fits ? wrap_once(G.org[2] + z, L.nf[2]) : wrap_idx(G.org[2] + z, L.nf[2]);
+          atomic_add_cplx_global(fwt + gx + (int64_t)L.nf[0] * (gy + (int64_t)L.nf[1] * gz), v);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Method 2 in 3D, exclusive-warp variant: one warp per block owns its tile, so
 // the tile is updated with plain shared-memory read-modify-writes instead of
 // atomics. Points arrive sorted by (bin, cell inside the bin); the contributions
@@ -312,11 +474,6 @@ template <typename T, int NS> struct Tile3W {
   static constexpr int NSLOT = NXB * NR;
   static constexpr bool MERGE = NS <= 8; // register accumulators for same-cell runs
 };
-
-// periodic index for i in [-n, 2n); used when the tile is not longer than the grid
-__device__ __forceinline__ int wrap_once(int i, int n) {
-  return i < 0 ? i + n : (i >= n ? i - n : i);
-}
 
 template <typename T, int NS>
 __global__ void __launch_bounds__(32)
@@ -588,19 +745,18 @@ __global__ void __launch_bounds__(GLOBAL_SPREAD_THREADS)
 // the fine grid (read through L1/L2: the points of a subproblem share a tile).
 constexpr int INTERP_THREADS = 128;
 
+// Interpolation: one thread per point; the point's kernel weights and grid
+// indices are computed once and reused for every transform of the batch.
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(INTERP_THREADS)
     interp_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ fw,
                   int64_t nf_total, const cplx<T> *__restrict__ post, int conj_post,
-                  cplx<T> *__restrict__ out) {
+                  cplx<T> *__restrict__ out, int ntr) {
   const int sub = blockIdx.x;
-  const int tr = blockIdx.y;
   const int b = L.sub_bin[sub];
   const int p0 = L.sub_start[sub];
   const int np = L.sub_count[sub];
   const TileGeom<DIM> G = tile_of<T, DIM, NS>(L, b);
-  const cplx<T> *fwt = fw + (int64_t)tr * nf_total;
-  cplx<T> *ot = out + (int64_t)tr * L.M;
   __shared__ T zst[DIM == 3 ? INTERP_THREADS * (NS + 1) : 1];
   __shared__ int zsti[DIM == 3 ? INTERP_THREADS * (NS + 1) : 1];
   for (int i = threadIdx.x; i < np; i += blockDim.x) {
@@ -614,45 +770,40 @@ __global__ void __launch_bounds__(INTERP_THREADS)
 #pragma unroll
       for (int a = 0; a < NS; ++a) gi[d][a] = wrap_idx(G.org[d] + s + a, L.nf[d]);
     }
-    T accr = T(0), acci = T(0);
-    if constexpr (DIM == 1) {
-#pragma unroll
-      for (int a = 0; a < NS; ++a) {
-        const cplx<T> g = __ldg(fwt + gi[0][a]);
-        accr = fma(g.x, ker[0][a], accr);
-        acci = fma(g.y, ker[0][a], acci);
-      }
-    } else if constexpr (DIM == 2) {
-#pragma unroll
-      for (int bb = 0; bb < NS; ++bb) {
-        const int64_t row = (int64_t)gi[DIM > 1 ? 1 : 0][bb] * L.nf[0];
-        T rr = T(0), ri = T(0);
-#pragma unroll
-        for (int a = 0; a < NS; ++a) {
-          const cplx<T> g = __ldg(fwt + row + gi[0][a]);
-          rr = fma(g.x, ker[0][a], rr);
-          ri = fma(g.y, ker[0][a], ri);
-        }
-        accr = fma(rr, ker[DIM > 1 ? 1 : 0][bb], accr);
-        acci = fma(ri, ker[DIM > 1 ? 1 : 0][bb], acci);
-      }
-    } else {
-      // z weights and rows go through shared memory: a dynamic index into a
+    T *kzs = zst + threadIdx.x * (NS + 1);
+    int *gzs = zsti + threadIdx.x * (NS + 1);
+    if constexpr (DIM == 3) {
+      // z weights and planes go through shared memory: a dynamic index into a
       // register array would put it in local memory
-      T *kzs = zst + threadIdx.x * (NS + 1);
-      int *gzs = reinterpret_cast<int *>(zsti) + threadIdx.x * (NS + 1);
 #pragma unroll
       for (int cc = 0; cc < NS; ++cc) {
         kzs[cc] = ker[DIM > 2 ? 2 : 0][cc];
         gzs[cc] = gi[DIM > 2 ? 2 : 0][cc];
       }
+    }
+    cplx<T> pf;
+    pf.x = T(1);
+    pf.y = T(0);
+    if (post) {
+      pf = post[j];
+      if (conj_post) pf.y = -pf.y;
+    }
 #pragma unroll 1
-      for (int cc = 0; cc < NS; ++cc) {
-        const int64_t plane = (int64_t)gzs[cc] * L.nf[0] * L.nf[1];
-        T pr = T(0), pi = T(0);
+    for (int tr = 0; tr < ntr; ++tr) {
+      const cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+      T accr = T(0), acci = T(0);
+      if constexpr (DIM == 1) {
 #pragma unroll
+        for (int a = 0; a < NS; ++a) {
+          const cplx<T> g = __ldg(fwt + gi[0][a]);
+          accr = fma(g.x, ker[0][a], accr);
+          acci = fma(g.y, ker[0][a], acci);
+        }
+      } else if constexpr (DIM == 2) {
+        constexpr int UB = NS > 8 ? 2 : NS; // bound the number of loads kept in flight
+#pragma unroll UB
         for (int bb = 0; bb < NS; ++bb) {
-          const int64_t row = plane + (int64_t)gi[DIM > 1 ? 1 : 0][bb] * L.nf[0];
+          const int64_t row = (int64_t)gi[DIM > 1 ? 1 : 0][bb] * L.nf[0];
           T rr = T(0), ri = T(0);
 #pragma unroll
           for (int a = 0; a < NS; ++a) {
@@ -660,18 +811,36 @@ __global__ void __launch_bounds__(INTERP_THREADS)
             rr = fma(g.x, ker[0][a], rr);
             ri = fma(g.y, ker[0][a], ri);
           }
-          pr = fma(rr, ker[DIM > 1 ? 1 : 0][bb], pr);
-          pi = fma(ri, ker[DIM > 1 ? 1 : 0][bb], pi);
+          accr = fma(rr, ker[DIM > 1 ? 1 : 0][bb], accr);
+          acci = fma(ri, ker[DIM > 1 ? 1 : 0][bb], acci);
         }
-        accr = fma(pr, kzs[cc], accr);
-        acci = fma(pi, kzs[cc], acci);
+      } else {
+#pragma unroll 1
+        for (int cc = 0; cc < NS; ++cc) {
+          const int64_t plane = (int64_t)gzs[cc] * L.nf[0] * L.nf[1];
+          T pr = T(0), pi = T(0);
+#pragma unroll
+          for (int bb = 0; bb < NS; ++bb) {
+            const int64_t row = plane + (int64_t)gi[DIM > 1 ? 1 : 0][bb] * L.nf[0];
+            T rr = T(0), ri = T(0);
+#pragma unroll
+            for (int a = 0; a < NS; ++a) {
+              const cplx<T> g = __ldg(fwt + row + gi[0][a]);
+              rr = fma(g.x, ker[0][a], rr);
+              ri = fma(g.y, ker[0][a], ri);
+            }
+            pr = fma(rr, ker[DIM > 1 ? 1 : 0][bb], pr);
+            pi = fma(ri, ker[DIM > 1 ? 1 : 0][bb], pi);
+          }
+          accr = fma(pr, kzs[cc], accr);
+          acci = fma(pi, kzs[cc], acci);
+        }
       }
+      cplx<T> r;
+      r.x = accr * pf.x - acci * pf.y;
+      r.y = accr * pf.y + acci * pf.x;
+      out[(int64_t)tr * L.M + j] = r;
     }
-    cplx<T> r;
-    r.x = accr;
-    r.y = acci;
-    if (post) r = cmul_opt<T>(r, post[j], conj_post);
-    ot[j] = r;
   }
 }
 
@@ -686,6 +855,14 @@ template <typename T, int DIM> struct Dispatch {
       spread_global_kernel<T, DIM, NS><<<grid, GLOBAL_SPREAD_THREADS, 0, s>>>(L, K, c, pre, conj_pre, fw,
                                                                     nf_total);
     } else if constexpr (DIM == 3) {
+      if (NS <= 8 && cfg.variant == 2) {
+        auto km = spread_tile3m_kernel<T, (NS <= 8 ? NS : 8)>;
+        GBN_CUDA(cudaFuncSetAttribute(km, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)cfg.smem));
+        km<<<grid, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
+        GBN_LAUNCH_CHECK();
+        return;
+      }
       if (cfg.variant == 1) {
         auto kw = spread_tile3w_kernel<T, NS>;
         GBN_CUDA(cudaFuncSetAttribute(kw, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -710,8 +887,8 @@ template <typename T, int DIM> struct Dispatch {
   static void interp(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *fw,
                      int64_t nf_total, const cplx<T> *post, int conj_post, cplx<T> *out,
                      int ntr, cudaStream_t s) {
-    dim3 grid((unsigned)L.nsub, (unsigned)ntr);
-    interp_kernel<T, DIM, NS><<<grid, INTERP_THREADS, 0, s>>>(L, K, fw, nf_total, post, conj_post, out);
+    interp_kernel<T, DIM, NS><<<(unsigned)L.nsub, INTERP_THREADS, 0, s>>>(L, K, fw, nf_total, post,
+                                                                         conj_post, out, ntr);
     GBN_LAUNCH_CHECK();
   }
 };
