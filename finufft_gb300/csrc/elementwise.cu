@@ -28,6 +28,12 @@ template <typename T> size_t spread_tile_smem(int dim, int ns, const int bin[3],
 template <typename T> size_t spread_tile3w_bytes(int ns, const int bin[3]) {
   return tile3_bytes<T>(ns, bin[0], bin[1], bin[2]) + t3w_stage_bytes(ns, (int)sizeof(T));
 }
+template <typename T> size_t spread_tile3m_bytes(int ns, const int bin[3], int warps) {
+  return tile3_bytes<T>(ns, bin[0], bin[1], bin[2]) +
+         (size_t)warps * t3m_stage_bytes(ns, (int)sizeof(T));
+}
+template size_t spread_tile3m_bytes<float>(int, const int[3], int);
+template size_t spread_tile3m_bytes<double>(int, const int[3], int);
 template size_t spread_tile3w_bytes<float>(int, const int[3]);
 template size_t spread_tile3w_bytes<double>(int, const int[3]);
 template size_t spread_tile_smem<float>(int, int, const int[3], int);

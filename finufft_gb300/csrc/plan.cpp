@@ -176,7 +176,15 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
     if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT")) variant = std::atoi(e);
     if (variant == 1 && wsm > (size_t)limit) variant = 2;
     if (variant < 0 || variant > 2 || (variant == 2 && ns > 8)) variant = 0;
+    const int mwarps = std::is_same_v<T, float> ? 12 : 8;
+    const size_t msm = spread_tile3m_bytes<T>(ns, bins, mwarps);
+    if (variant == 2 && msm > (size_t)limit) variant = 0;
     S.cfg.variant = variant;
+    if (variant == 2) {
+      S.cfg.threads = 32 * mwarps;
+      S.cfg.smem = msm;
+      S.smem = msm;
+    }
     if (variant == 1) {
       S.cfg.threads = 32;
       S.cfg.smem = wsm;

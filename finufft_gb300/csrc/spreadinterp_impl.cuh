@@ -300,6 +300,12 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// threads of the warp-aggregated 3D spread: 12 warps share a tile in single
+// precision, 8 in double (twice the accumulator registers); 2 blocks per SM
+template <typename T> __host__ __device__ constexpr int t3m_threads() {
+  return sizeof(T) == 8 ? 256 : 384;
+}
+
 // ---------------------------------------------------------------------------
 // Method 2 in 3D, warp-aggregated variant: the tile is shared by the block's
 // warps (atomics, as in spread_tile3_kernel), but each warp takes a contiguous
@@ -308,7 +314,7 @@ __global__ void __launch_bounds__(256)
 // atomics once per run instead of once per point. Staging and lane mapping
 // are those of spread_tile3_kernel.
 template <typename T, int NS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(t3m_threads<T>(), 2)
     spread_tile3m_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
                          const cplx<T> *__restrict__ pre, int conj_pre,
                          cplx<T> *__restrict__ fw, int64_t nf_total) {
@@ -330,11 +336,12 @@ __global__ void __launch_bounds__(256)
   T *re = reinterpret_cast<T *>(smem_raw);
   T *im = re + Q * G.t[2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  unsigned char *stage = smem_raw + tile_bytes + (size_t)warp * stage_bytes_per_warp<T>(NS);
-  T *kx = reinterpret_cast<T *>(stage);
-  T *ky = kx + NS * SK;
-  T *kz = ky + NS * SK;
-  T *vre = kz + NS * SK;
+  // per-warp staging: x weights, (y,z) weight products (NS*NS rows padded to
+  // 4*NR), strengths and packed start cells of 32 points
+  T *kx = reinterpret_cast<T *>(smem_raw + tile_bytes +
+                                (size_t)warp * t3m_stage_bytes(NS, (int)sizeof(T)));
+  T *yz = kx + NS * SK;
+  T *vre = yz + 4 * NR * SK;
   T *vim = vre + SK;
   int *spk = reinterpret_cast<int *>(vim + SK);
   {
@@ -344,18 +351,15 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   const int lx = lane & 7, lp = lane >> 3;
-  int off[NSLOT], iy[NSLOT], iz[NSLOT];
+  int off[NSLOT];
   bool ok[NSLOT];
 #pragma unroll
   for (int xb = 0; xb < NXB; ++xb)
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
       const int pp = 4 * r + lp, dx = 8 * xb + lx, k = xb * NR + r;
-      const int dy = pp % NS, dz = pp / NS;
       ok[k] = dx < NS && pp < NS * NS;
-      iy[k] = (ok[k] ? dy : 0) * SK;
-      iz[k] = (ok[k] ? dz : 0) * SK;
-      off[k] = dz * Q + dy * px + dx;
+      off[k] = (pp / NS) * Q + (pp % NS) * px + dx;
     }
   T ar[NSLOT], ai[NSLOT];
   int cur = -1;
@@ -363,6 +367,8 @@ __global__ void __launch_bounds__(256)
   const int per = (np + nwarp - 1) / nwarp;
   const int w0 = min(np, warp * per), w1 = min(np, w0 + per);
   const cplx<T> *ct = c + (int64_t)tr * L.M;
+  const T *kxl = kx + lx * SK;       // this lane's x weight row (x chunk 0)
+  const T *yzl = yz + lp * SK;       // this lane's first (y,z) pair row
   for (int base = w0; base < w1; base += 32) {
     const int i = base + lane;
     if (i < w1) {
@@ -370,16 +376,16 @@ __global__ void __launch_bounds__(256)
       const int j = L.perm[p];
       cplx<T> v = ct[j];
       if (pre) v = cmul_opt<T>(v, pre[j], conj_pre);
-      T kk[NS];
-      const int sx = point_weights<T, NS>(L.loc[0][p], L.bin[0], K, kk);
+      T ka[NS], kb[NS], kc[NS];
+      const int sx = point_weights<T, NS>(L.loc[0][p], L.bin[0], K, ka);
+      const int sy = point_weights<T, NS>(L.loc[1][p], L.bin[1], K, kb);
+      const int sz = point_weights<T, NS>(L.loc[2][p], L.bin[2], K, kc);
 #pragma unroll
-      for (int a = 0; a < NS; ++a) kx[a * SK + lane] = kk[a];
-      const int sy = point_weights<T, NS>(L.loc[1][p], L.bin[1], K, kk);
+      for (int a = 0; a < NS; ++a) kx[a * SK + lane] = ka[a];
 #pragma unroll
-      for (int a = 0; a < NS; ++a) ky[a * SK + lane] = kk[a];
-      const int sz = point_weights<T, NS>(L.loc[2][p], L.bin[2], K, kk);
+      for (int zz = 0; zz < NS; ++zz)
 #pragma unroll
-      for (int a = 0; a < NS; ++a) kz[a * SK + lane] = kk[a];
+        for (int yy = 0; yy < NS; ++yy) yz[(zz * NS + yy) * SK + lane] = kb[yy] * kc[zz];
       vre[lane] = v.x;
       vim[lane] = v.y;
       spk[lane] = sx | (sy << 10) | (sz << 20);
@@ -405,14 +411,13 @@ __global__ void __launch_bounds__(256)
       const T vr = vre[q], vi = vim[q];
 #pragma unroll
       for (int xb = 0; xb < NXB; ++xb) {
-        const T wx = kx[(8 * xb + lx) * SK + q]; // x offsets >= NS read staged y weights
+        const T wx = kxl[8 * xb * SK + q]; // x offsets >= NS read staged products (unused)
         const T xr = vr * wx, xi = vi * wx;
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
-          const int k = xb * NR + r;
-          const T w = ky[iy[k] + q] * kz[iz[k] + q];
-          ar[k] = fma(xr, w, ar[k]);
-          ai[k] = fma(xi, w, ai[k]);
+          const T w = yzl[4 * r * SK + q];
+          ar[xb * NR + r] = fma(xr, w, ar[xb * NR + r]);
+          ai[xb * NR + r] = fma(xi, w, ai[xb * NR + r]);
         }
       }
     }
@@ -428,7 +433,7 @@ __global__ void __launch_bounds__(256)
       }
   }
   __syncthreads();
-  // write back: lanes cover (x, row) pairs, rows of tx cells
+  // write back: lanes cover (x, row) pairs; rows advance by a fixed stride
   cplx<T> *fwt = fw + (int64_t)tr * nf_total;
   const int tx = G.t[0], ty = G.t[1], tz = G.t[2];
   const bool fits = tx <= L.nf[0] && ty <= L.nf[1] && tz <= L.nf[2] && NS <= 2 * L.nf[0] &&
@@ -437,11 +442,14 @@ __global__ void __launch_bounds__(256)
   while (txp < tx && txp < 32) txp <<= 1;
   const int rows_per = blockDim.x / txp;
   const int rows = ty * tz;
+  const int64_t plane = (int64_t)L.nf[0] * L.nf[1];
   for (int x0 = 0; x0 < tx; x0 += txp) {
     const int x = x0 + (threadIdx.x & (txp - 1));
     const int gx = fits ? wrap_once(G.org[0] + x, L.nf[0]) : wrap_idx(G.org[0] + x, L.nf[0]);
-    for (int r0 = threadIdx.x / txp; r0 < rows; r0 += rows_per) {
-      const int y = r0 % ty, z = r0 / ty;
+    int r0 = threadIdx.x / txp;
+    int y = r0 % ty, z = r0 / ty; // advanced incrementally below
+    const int dy = rows_per % ty, dz = rows_per / ty;
+    for (; r0 < rows; r0 += rows_per) {
       if (x < tx) {
         const int sidx = z * Q + y * px + x;
         cplx<T> v;
@@ -450,8 +458,14 @@ __global__ void __launch_bounds__(256)
         if (v.x != T(0) || v.y != T(0)) {
           const int gy = fits ? wrap_once(G.org[1] + y, L.nf[1]) : wrap_idx(G.org[1] + y, L.nf[1]);
           const int gz = fits ? wrap_once(G.org[2] + z, L.nf[2]) : wrap_idx(G.org[2] + z, L.nf[2]);
-          atomic_add_cplx_global(fwt + gx + (int64_t)L.nf[0] * (gy + (int64_t)L.nf[1] * gz), v);
+          atomic_add_cplx_global(fwt + gx + (int64_t)L.nf[0] * gy + plane * gz, v);
         }
+      }
+      y += dy;
+      z += dz;
+      if (y >= ty) {
+        y -= ty;
+        ++z;
       }
     }
   }
@@ -859,7 +873,7 @@ template <typename T, int DIM> struct Dispatch {
         auto km = spread_tile3m_kernel<T, (NS <= 8 ? NS : 8)>;
         GBN_CUDA(cudaFuncSetAttribute(km, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)cfg.smem));
-        km<<<grid, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
+        km<<<grid, t3m_threads<T>(), cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
         GBN_LAUNCH_CHECK();
         return;
       }

@@ -34,4 +34,10 @@ __host__ __device__ constexpr int t3w_stage_bytes(int ns, int tsize) {
           (t3w_chunk(ns, tsize) + 1) * 4 + 15) / 16 * 16;
 }
 
+// Warp-aggregated 3D spread: staging of one warp (x weights, (y,z) weight
+// products padded to 4*ceil(ns^2/4) rows, strengths, packed start cells).
+__host__ __device__ constexpr int t3m_stage_bytes(int ns, int tsize) {
+  return (33 * (ns + 4 * ((ns * ns + 3) / 4) + 2) * tsize + 33 * 4 + 15) / 16 * 16;
+}
+
 } // namespace gbn
