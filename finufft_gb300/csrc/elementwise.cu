@@ -32,6 +32,14 @@ template <typename T> size_t spread_tile3m_bytes(int ns, const int bin[3], int w
   return tile3_bytes<T>(ns, bin[0], bin[1], bin[2]) +
          (size_t)warps * t3m_stage_bytes(ns, (int)sizeof(T));
 }
+template <typename T> size_t spread_tile2m_bytes(int ns, const int bin[3]) {
+  const size_t tile = (2 * sizeof(T) * (size_t)tile_pitch_x(3, bin[0] + ns) * (bin[1] + ns) + 15) /
+                      16 * 16;
+  const size_t stage = (33 * (2 * ns + 2) * sizeof(T) + 33 * 4 + 15) / 16 * 16;
+  return tile + 8 * stage;
+}
+template size_t spread_tile2m_bytes<float>(int, const int[3]);
+template size_t spread_tile2m_bytes<double>(int, const int[3]);
 template size_t spread_tile3m_bytes<float>(int, const int[3], int);
 template size_t spread_tile3m_bytes<double>(int, const int[3], int);
 template size_t spread_tile3w_bytes<float>(int, const int[3]);

@@ -672,6 +672,152 @@ __global__ void __launch_bounds__(32)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Method 2 in 2D, warp-aggregated: the 2D analogue of spread_tile3m_kernel.
+// Lanes (lx, ly) = (lane & 7, lane >> 3) cover an 8-cell x run of 4 rows; the
+// row pitch is 8 mod 16 words so the 4 rows fall in disjoint bank octets.
+// Points are (bin, cell)-sorted; each warp sums runs of points sharing their
+// first support cell in registers and adds them to the tile once per run.
+template <typename T> __host__ __device__ constexpr int t2m_stage_bytes(int ns) {
+  return (33 * (2 * ns + 2) * (int)sizeof(T) + 33 * 4 + 15) / 16 * 16;
+}
+template <typename T> __host__ __device__ constexpr size_t tile2m_bytes(int ns, int bx, int by) {
+  return (2 * sizeof(T) * (size_t)tile_pitch_x(3, bx + ns) * (by + ns) + 15) / 16 * 16;
+}
+
+template <typename T, int NS>
+__global__ void __launch_bounds__(256)
+    spread_tile2m_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
+                         const cplx<T> *__restrict__ pre, int conj_pre,
+                         cplx<T> *__restrict__ fw, int64_t nf_total) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int SK = STAGE_STRIDE;
+  constexpr int NXB = (NS + 7) / 8;
+  constexpr int NRY = (NS + 3) / 4;
+  constexpr int NSLOT = NXB * NRY;
+  const int sub = blockIdx.x, tr = blockIdx.y;
+  const int b = L.sub_bin[sub];
+  const int p0 = L.sub_start[sub];
+  const int np = L.sub_count[sub];
+  const TileGeom<2> G = tile_of<T, 2, NS>(L, b);
+  const int px = tile_pitch_x(3, G.t[0]);
+  const size_t tile_bytes = tile2m_bytes<T>(NS, L.bin[0], L.bin[1]);
+  T *re = reinterpret_cast<T *>(smem_raw);
+  T *im = re + px * G.t[1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  T *kx = reinterpret_cast<T *>(smem_raw + tile_bytes + (size_t)warp * t2m_stage_bytes<T>(NS));
+  T *ky = kx + NS * SK;
+  T *vre = ky + NS * SK;
+  T *vim = vre + SK;
+  int *spk = reinterpret_cast<int *>(vim + SK);
+  {
+    uint4 *z4 = reinterpret_cast<uint4 *>(smem_raw);
+    const uint4 zero = make_uint4(0, 0, 0, 0);
+    for (int i = threadIdx.x; i < (int)(tile_bytes / 16); i += blockDim.x) z4[i] = zero;
+  }
+  __syncthreads();
+  const int lx = lane & 7, ly = lane >> 3;
+  int off[NSLOT];
+  bool ok[NSLOT];
+#pragma unroll
+  for (int xb = 0; xb < NXB; ++xb)
+#pragma unroll
+    for (int r = 0; r < NRY; ++r) {
+      const int dx = 8 * xb + lx, dy = 4 * r + ly, k = xb * NRY + r;
+      ok[k] = dx < NS && dy < NS;
+      off[k] = dy * px + dx;
+    }
+  T ar[NSLOT], ai[NSLOT];
+  int cur = -1;
+  const int per = (np + nwarp - 1) / nwarp;
+  const int w0 = min(np, warp * per), w1 = min(np, w0 + per);
+  const cplx<T> *ct = c + (int64_t)tr * L.M;
+  const T *kxl = kx + lx * SK;
+  const T *kyl = ky + ly * SK;
+  for (int base = w0; base < w1; base += 32) {
+    const int i = base + lane;
+    if (i < w1) {
+      const int p = p0 + i;
+      const int j = L.perm[p];
+      cplx<T> v = ct[j];
+      if (pre) v = cmul_opt<T>(v, pre[j], conj_pre);
+      T kk[NS];
+      const int sx = point_weights<T, NS>(L.loc[0][p], L.bin[0], K, kk);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) kx[a * SK + lane] = kk[a];
+      const int sy = point_weights<T, NS>(L.loc[1][p], L.bin[1], K, kk);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) ky[a * SK + lane] = kk[a];
+      vre[lane] = v.x;
+      vim[lane] = v.y;
+      spk[lane] = sx | (sy << 16);
+    }
+    __syncwarp();
+    const int cnt = min(32, w1 - base);
+    for (int q = 0; q < cnt; ++q) {
+      const int sp = spk[q];
+      if (sp != cur) {
+        if (cur >= 0) {
+          const int rb = (cur >> 16) * px + (cur & 0xffff);
+#pragma unroll
+          for (int k = 0; k < NSLOT; ++k)
+            if (ok[k]) {
+              atomicAdd(re + rb + off[k], ar[k]);
+              atomicAdd(im + rb + off[k], ai[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NSLOT; ++k) ar[k] = ai[k] = T(0);
+        cur = sp;
+      }
+      const T vr = vre[q], vi = vim[q];
+#pragma unroll
+      for (int xb = 0; xb < NXB; ++xb) {
+        const T wx = kxl[8 * xb * SK + q]; // x offsets >= NS read staged y weights (unused)
+        const T xr = vr * wx, xi = vi * wx;
+#pragma unroll
+        for (int r = 0; r < NRY; ++r) {
+          const T w = kyl[4 * r * SK + q];
+          ar[xb * NRY + r] = fma(xr, w, ar[xb * NRY + r]);
+          ai[xb * NRY + r] = fma(xi, w, ai[xb * NRY + r]);
+        }
+      }
+    }
+    __syncwarp();
+  }
+  if (cur >= 0) {
+    const int rb = (cur >> 16) * px + (cur & 0xffff);
+#pragma unroll
+    for (int k = 0; k < NSLOT; ++k)
+      if (ok[k]) {
+        atomicAdd(re + rb + off[k], ar[k]);
+        atomicAdd(im + rb + off[k], ai[k]);
+      }
+  }
+  __syncthreads();
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  const int tx = G.t[0], ty = G.t[1];
+  const bool fits = tx <= L.nf[0] && ty <= L.nf[1] && NS <= 2 * L.nf[0] && NS <= 2 * L.nf[1];
+  int txp = 1;
+  while (txp < tx && txp < 32) txp <<= 1;
+  const int rows_per = blockDim.x / txp;
+  for (int x0 = 0; x0 < tx; x0 += txp) {
+    const int x = x0 + (threadIdx.x & (txp - 1));
+    const int gx = fits ? wrap_once(G.org[0] + x, L.nf[0]) : wrap_idx(G.org[0] + x, L.nf[0]);
+    for (int y = threadIdx.x / txp; y < ty; y += rows_per) {
+      if (x < tx) {
+        cplx<T> v;
+        v.x = re[y * px + x];
+        v.y = im[y * px + x];
+        if (v.x != T(0) || v.y != T(0)) {
+          const int gy = fits ? wrap_once(G.org[1] + y, L.nf[1]) : wrap_idx(G.org[1] + y, L.nf[1]);
+          atomic_add_cplx_global(fwt + gx + (int64_t)L.nf[0] * gy, v);
+        }
+      }
+    }
+  }
+}
+
 // Method 1: point-driven spreading straight into global memory with vector
 // atomics (no tile). Points are still processed in bin order for locality.
 constexpr int GLOBAL_SPREAD_THREADS = 128;
@@ -889,6 +1035,11 @@ template <typename T, int DIM> struct Dispatch {
       GBN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)cfg.smem));
       kern<<<grid, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
+    } else if (DIM == 2 && cfg.variant == 2) {
+      auto k2 = spread_tile2m_kernel<T, NS>;
+      GBN_CUDA(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)cfg.smem));
+      k2<<<grid, 256, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
     } else {
       auto kern = spread_tile_kernel<T, DIM, NS>;
       GBN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
