@@ -127,6 +127,20 @@ def _declare(lib):
     lib.finufft_default_opts.argtypes = [POINTER(FinufftOpts)]
     lib.finufft_default_opts.restype = None
     lib.gbnufft_version.restype = ctypes.c_char_p
+    for pfx, real in (("cufinufft", c_double), ("cufinufftf", c_float)):
+        f = getattr(lib, pfx + "_batch_makeplan")
+        f.argtypes = [c_int, c_int, c_int, i64p, c_int, real, POINTER(c_void_p),
+                      POINTER(CufinufftOpts), POINTER(GbnufftOpts)]
+        f.restype = c_int
+        f = getattr(lib, pfx + "_batch_setpts")
+        f.argtypes = [c_void_p, i64p, c_void_p, c_void_p, c_void_p]
+        f.restype = c_int
+        f = getattr(lib, pfx + "_batch_execute")
+        f.argtypes = [c_void_p, c_void_p, c_void_p]
+        f.restype = c_int
+        f = getattr(lib, pfx + "_batch_destroy")
+        f.argtypes = [c_void_p]
+        f.restype = c_int
     lib.cufinufftf_spread_noalloc.argtypes = [c_int, POINTER(c_int64), c_int64, c_void_p,
                                               c_void_p, c_void_p, c_void_p, c_void_p, c_float,
                                               c_void_p]

@@ -29,6 +29,7 @@ CU_SOURCES = [
     "spreadinterp_2d.cu",
     "spreadinterp_3d.cu",
     "noalloc.cu",
+    "batch.cu",
 ]
 CPP_SOURCES = ["planning.cpp", "plan.cpp", "c_api.cpp", "host_api.cpp"]
 

@@ -64,6 +64,16 @@ template <typename T> struct KernelShape {
 
 // Where the nonuniform points sit after the device bin sort, and how the
 // fine grid is tiled. Passed by value to spread/interp kernels.
+// One problem of a batch of independent transforms (batched execution): its
+// fine grid, bin counts, first global bin and grid offset.
+struct BatchProb {
+  int nf[3];
+  int nbin[3];
+  int binoff;   // first global bin of this problem
+  int pad_;
+  int64_t gridoff; // offset of its fine grid in the batch's grid array
+};
+
 template <typename T> struct PointLayout {
   int dim;
   int nf[3];       // fine grid size per dimension
@@ -76,6 +86,10 @@ template <typename T> struct PointLayout {
   const int *sub_count; // subproblem -> number of points
   const int *perm;      // sorted position -> user index
   const T *loc[3];      // sorted bin-local coordinates in grid units, [0, bin]
+  // batched execution: subproblem bins are global; binprob maps them to
+  // problems, whose grids and bin counts replace nf/nbin above (null otherwise)
+  const BatchProb *probs = nullptr;
+  const int *binprob = nullptr;
 };
 
 } // namespace gbn

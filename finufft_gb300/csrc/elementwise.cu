@@ -35,7 +35,7 @@ template <typename T> size_t spread_tile3m_bytes(int ns, const int bin[3], int w
 template <typename T> size_t spread_tile2m_bytes(int ns, const int bin[3]) {
   const size_t tile = (2 * sizeof(T) * (size_t)tile_pitch_x(3, bin[0] + ns) * (bin[1] + ns) + 15) /
                       16 * 16;
-  const size_t stage = (33 * (2 * ns + 2) * sizeof(T) + 33 * 4 + 15) / 16 * 16;
+  const size_t stage = (33 * (ns + 4 * ((ns + 3) / 4) + 2) * sizeof(T) + 33 * 4 + 15) / 16 * 16;
   return tile + 8 * stage;
 }
 template size_t spread_tile2m_bytes<float>(int, const int[3]);

@@ -53,6 +53,24 @@ __device__ __forceinline__ int wrap_once(int i, int n) {
   return i < 0 ? i + n : (i >= n ? i - n : i);
 }
 
+// Geometry of the problem a subproblem belongs to: for a batch, replaces the
+// layout's grid and bin counts by the problem's and returns its grid offset;
+// b becomes the bin index inside the problem.
+template <typename T>
+__device__ __forceinline__ int64_t resolve_problem(const PointLayout<T> &L, PointLayout<T> &Lb,
+                                                   int &b) {
+  Lb = L;
+  if (!L.probs) return 0;
+  const BatchProb P = L.probs[L.binprob[b]];
+  b -= P.binoff;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    Lb.nf[d] = P.nf[d];
+    Lb.nbin[d] = P.nbin[d];
+  }
+  return P.gridoff;
+}
+
 // first support cell (tile coordinates) and kernel weights of one point
 template <typename T, int NS>
 __device__ __forceinline__ int point_weights(T l, int binsz, const KernelShape<T> &K, T *ker) {
@@ -71,13 +89,16 @@ __device__ __forceinline__ int point_weights(T l, int binsz, const KernelShape<T
 // distinct banks (row pitch = 8 mod 32). 1D and 2D use one thread per point.
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(256)
-    spread_tile_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
+    spread_tile_kernel(PointLayout<T> L0, KernelShape<T> K, const cplx<T> *__restrict__ c,
                        const cplx<T> *__restrict__ pre, int conj_pre,
                        cplx<T> *__restrict__ fw, int64_t nf_total) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int sub = blockIdx.x;
   const int tr = blockIdx.y;
-  const int b = L.sub_bin[sub];
+  int b = L0.sub_bin[sub];
+  PointLayout<T> Lg;
+  const int64_t goff = resolve_problem<T>(L0, Lg, b);
+  const PointLayout<T> &L = Lg;
   const int p0 = L.sub_start[sub];
   const int np = L.sub_count[sub];
   const TileGeom<DIM> G = tile_of<T, DIM, NS>(L, b);
@@ -165,7 +186,7 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   // write the tile back: every tile cell adds into its periodic image
-  cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total + goff;
   for (int q = threadIdx.x; q < G.cells; q += blockDim.x) {
     const int x = q % G.t[0];
     const int y = (q / G.t[0]) % G.t[1];
@@ -315,7 +336,7 @@ template <typename T> __host__ __device__ constexpr int t3m_threads() {
 // are those of spread_tile3_kernel.
 template <typename T, int NS>
 __global__ void __launch_bounds__(t3m_threads<T>(), 2)
-    spread_tile3m_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
+    spread_tile3m_kernel(PointLayout<T> L0, KernelShape<T> K, const cplx<T> *__restrict__ c,
                          const cplx<T> *__restrict__ pre, int conj_pre,
                          cplx<T> *__restrict__ fw, int64_t nf_total) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -325,7 +346,10 @@ __global__ void __launch_bounds__(t3m_threads<T>(), 2)
   constexpr int NSLOT = NXB * NR;
   const int sub = blockIdx.x;
   const int tr = blockIdx.y;
-  const int b = L.sub_bin[sub];
+  int b = L0.sub_bin[sub];
+  PointLayout<T> Lg;
+  const int64_t goff = resolve_problem<T>(L0, Lg, b);
+  const PointLayout<T> &L = Lg;
   const int p0 = L.sub_start[sub];
   const int np = L.sub_count[sub];
   const TileGeom<3> G = tile_of<T, 3, NS>(L, b);
@@ -434,7 +458,7 @@ __global__ void __launch_bounds__(t3m_threads<T>(), 2)
   }
   __syncthreads();
   // write back: lanes cover (x, row) pairs; rows advance by a fixed stride
-  cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total + goff;
   const int tx = G.t[0], ty = G.t[1], tz = G.t[2];
   const bool fits = tx <= L.nf[0] && ty <= L.nf[1] && tz <= L.nf[2] && NS <= 2 * L.nf[0] &&
                     NS <= 2 * L.nf[1] && NS <= 2 * L.nf[2];
@@ -678,8 +702,10 @@ __global__ void __launch_bounds__(32)
 // row pitch is 8 mod 16 words so the 4 rows fall in disjoint bank octets.
 // Points are (bin, cell)-sorted; each warp sums runs of points sharing their
 // first support cell in registers and adds them to the tile once per run.
+// staging: x weights (ns rows), y weights padded to 4*ceil(ns/4) rows (lanes
+// read rows 4r + ly up to that bound), strengths, packed start cells
 template <typename T> __host__ __device__ constexpr int t2m_stage_bytes(int ns) {
-  return (33 * (2 * ns + 2) * (int)sizeof(T) + 33 * 4 + 15) / 16 * 16;
+  return (33 * (ns + 4 * ((ns + 3) / 4) + 2) * (int)sizeof(T) + 33 * 4 + 15) / 16 * 16;
 }
 template <typename T> __host__ __device__ constexpr size_t tile2m_bytes(int ns, int bx, int by) {
   return (2 * sizeof(T) * (size_t)tile_pitch_x(3, bx + ns) * (by + ns) + 15) / 16 * 16;
@@ -687,7 +713,7 @@ template <typename T> __host__ __device__ constexpr size_t tile2m_bytes(int ns, 
 
 template <typename T, int NS>
 __global__ void __launch_bounds__(256)
-    spread_tile2m_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
+    spread_tile2m_kernel(PointLayout<T> L0, KernelShape<T> K, const cplx<T> *__restrict__ c,
                          const cplx<T> *__restrict__ pre, int conj_pre,
                          cplx<T> *__restrict__ fw, int64_t nf_total) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -696,7 +722,10 @@ __global__ void __launch_bounds__(256)
   constexpr int NRY = (NS + 3) / 4;
   constexpr int NSLOT = NXB * NRY;
   const int sub = blockIdx.x, tr = blockIdx.y;
-  const int b = L.sub_bin[sub];
+  int b = L0.sub_bin[sub];
+  PointLayout<T> Lg;
+  const int64_t goff = resolve_problem<T>(L0, Lg, b);
+  const PointLayout<T> &L = Lg;
   const int p0 = L.sub_start[sub];
   const int np = L.sub_count[sub];
   const TileGeom<2> G = tile_of<T, 2, NS>(L, b);
@@ -707,7 +736,7 @@ __global__ void __launch_bounds__(256)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   T *kx = reinterpret_cast<T *>(smem_raw + tile_bytes + (size_t)warp * t2m_stage_bytes<T>(NS));
   T *ky = kx + NS * SK;
-  T *vre = ky + NS * SK;
+  T *vre = ky + 4 * NRY * SK;
   T *vim = vre + SK;
   int *spk = reinterpret_cast<int *>(vim + SK);
   {
@@ -795,7 +824,7 @@ __global__ void __launch_bounds__(256)
       }
   }
   __syncthreads();
-  cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total + goff;
   const int tx = G.t[0], ty = G.t[1];
   const bool fits = tx <= L.nf[0] && ty <= L.nf[1] && NS <= 2 * L.nf[0] && NS <= 2 * L.nf[1];
   int txp = 1;
@@ -909,11 +938,14 @@ constexpr int INTERP_THREADS = 128;
 // indices are computed once and reused for every transform of the batch.
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(INTERP_THREADS)
-    interp_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ fw,
+    interp_kernel(PointLayout<T> L0, KernelShape<T> K, const cplx<T> *__restrict__ fw,
                   int64_t nf_total, const cplx<T> *__restrict__ post, int conj_post,
                   cplx<T> *__restrict__ out, int ntr) {
   const int sub = blockIdx.x;
-  const int b = L.sub_bin[sub];
+  int b = L0.sub_bin[sub];
+  PointLayout<T> Lg;
+  const int64_t goff = resolve_problem<T>(L0, Lg, b);
+  const PointLayout<T> &L = Lg;
   const int p0 = L.sub_start[sub];
   const int np = L.sub_count[sub];
   const TileGeom<DIM> G = tile_of<T, DIM, NS>(L, b);
@@ -950,7 +982,7 @@ __global__ void __launch_bounds__(INTERP_THREADS)
     }
 #pragma unroll 1
     for (int tr = 0; tr < ntr; ++tr) {
-      const cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+      const cplx<T> *fwt = fw + (int64_t)tr * nf_total + goff;
       T accr = T(0), acci = T(0);
       if constexpr (DIM == 1) {
 #pragma unroll

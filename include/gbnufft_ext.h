@@ -69,6 +69,28 @@ GBNUFFT_EXPORT void gbnufft_default_opts(gbnufft_opts *o);
 GBNUFFT_EXT_DECLS(cufinufft, cufinufft_plan, double, cuDoubleComplex)
 GBNUFFT_EXT_DECLS(cufinufftf, cufinufftf_plan, float, cuFloatComplex)
 
+/* Uneven batches: nprob independent transforms of one type (1 or 2) and
+ * dimension with different mode counts and point sets, executed by one sort,
+ * one spread/interpolation launch over all problems, cuFFT batched over
+ * problems of equal grid shape and one deconvolution launch. n_modes holds
+ * 3 int64 per problem (x fastest; unused dimensions ignored). M holds the
+ * point count of each problem (host array); x/y/z, c and fk are concatenated
+ * device arrays in problem order (c: sum M strengths; fk: sum prod(n_modes)).
+ * ext may be NULL. */
+typedef struct cufinufft_batch_s *cufinufft_batch_plan;
+typedef struct cufinufftf_batch_s *cufinufftf_batch_plan;
+#define GBNUFFT_BATCH_DECLS(P, PLAN, T, C)                                                 \
+  GBNUFFT_EXPORT int P##_batch_makeplan(int type, int dim, int nprob,                    \
+                                        const int64_t *n_modes, int iflag, T eps,        \
+                                        PLAN *plan, const cufinufft_opts *opts,          \
+                                        const gbnufft_opts *ext);                        \
+  GBNUFFT_EXPORT int P##_batch_setpts(PLAN plan, const int64_t *M, const T *d_x,         \
+                                      const T *d_y, const T *d_z);                       \
+  GBNUFFT_EXPORT int P##_batch_execute(PLAN plan, C *d_c, C *d_fk);                      \
+  GBNUFFT_EXPORT int P##_batch_destroy(PLAN plan);
+GBNUFFT_BATCH_DECLS(cufinufft, cufinufft_batch_plan, double, cuDoubleComplex)
+GBNUFFT_BATCH_DECLS(cufinufftf, cufinufftf_batch_plan, float, cuFloatComplex)
+
 /* Measures the device's conflict-free shared-memory f32 atomicAdd rate
  * (lane operations per second), the peak the spreading kernels are held to. */
 GBNUFFT_EXPORT int gbnufft_smem_atomic_rate(int device, double *rate);
