@@ -307,6 +307,141 @@ def cpu_baseline(m_sample, seed):
                       % (m_sample, t_spread, t_fixed)}
 
 
+def _timed(fn, stream, steps, warmup):
+    return time_steps(fn, stream, steps, warmup)
+
+
+def run_config(args):
+    """Secondary configurations (one JSON line each; not the metric line)."""
+    import torch
+
+    import finufft_gb300 as fg
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    g = torch.Generator(device="cuda").manual_seed(11)
+    out = {"config_name": args.config, "n_gpus": 1, "data": "synthetic (seeded)"}
+    if args.config == "c1":
+        # 1D type 1, FP64: M = N = 1e6, tol 1e-9
+        M, N = 1_000_000, 1_000_000
+        x = (torch.rand(M, generator=g, device="cuda", dtype=torch.float64) * 2 - 1) * np.pi
+        c = torch.randn(M, 2, generator=g, device="cuda", dtype=torch.float64).view(torch.complex128)[:, 0]
+        p = fg.Plan(1, (N,), eps=1e-9, dtype="complex128", gpu_stream=stream.cuda_stream)
+        p.setpts(x)
+        f = torch.empty(N, dtype=torch.complex128, device=dev)
+        ms = _timed(lambda: p.execute(c, out=f), stream, args.steps, args.warmup)
+        out.update({"workload": "1D type 1 FP64, M=N=1e6, tol 1e-9", "value": M / (ms * 1e-3),
+                    "unit": "NU pts/s", "ms_per_step": ms})
+    elif args.config == "c2":
+        # 2D type 2 batched: N = 1024^2, ntransf 16, M = 1e7, tol 1e-5, iflag -1
+        M, nt, N = 10_000_000, 16, (1024, 1024)
+        x, y = ((torch.rand(2, M, generator=g, device="cuda", dtype=torch.float64) * 2 - 1)
+                * np.pi).to(torch.float32)
+        fk = torch.randn(nt, *N, 2, generator=g, device="cuda").view(torch.complex64)[..., 0]
+        p1 = fg.Plan(2, N, eps=1e-5, isign=-1, gpu_stream=stream.cuda_stream)
+        p1.setpts(x, y)
+        c1 = torch.empty(M, dtype=torch.complex64, device=dev)
+        f0 = fk[0].contiguous()
+        ms1 = _timed(lambda: p1.execute(f0, out=c1), stream, args.steps, args.warmup)
+        pb = fg.Plan(2, N, n_trans=nt, eps=1e-5, isign=-1, gpu_stream=stream.cuda_stream,
+                     gpu_maxbatchsize=nt)
+        pb.setpts(x, y)
+        cb = torch.empty(nt, M, dtype=torch.complex64, device=dev)
+        pb.execute(fk, out=cb)
+        torch.cuda.synchronize()
+        pb.graph_capture(cb, fk)
+        msb = _timed(pb.graph_launch, stream, args.steps, args.warmup)
+        pb.stage_times(True)
+        pb.execute(fk, out=cb)
+        torch.cuda.synchronize()
+        st = pb.stage_times(True)
+        # interp roofline: grid bytes read per transform + coordinates + output
+        nf = pb.info().nf
+        interp_bytes = nt * nf[0] * nf[1] * 8 + M * 2 * 4 + nt * M * 8
+        out.update({"workload": "2D type 2 FP32, N=1024^2, 16 vectors, M=1e7, tol 1e-5",
+                    "value": M * nt / (msb * 1e-3), "unit": "NU pts/s", "ms_per_step": msb,
+                    "plain": {"value": M / (ms1 * 1e-3), "ms_per_step": ms1},
+                    "batched_stage_ms": {"interp": st[0], "fft": st[1], "amplify": st[2],
+                                         "total": st[3]},
+                    "interp_hbm_GBps_algorithmic": interp_bytes / (st[0] * 1e-3) / 1e9})
+    elif args.config == "c4":
+        # 4096 uneven 2D type 1 problems, tol 1e-6, one batched plan
+        import ctypes
+
+        rng = np.random.default_rng(4)
+        nprob = 4096
+        Ns = np.round(np.exp(rng.uniform(np.log(32), np.log(256), (nprob, 2)))).astype(np.int64)
+        Ms = np.round(np.exp(rng.uniform(np.log(1e3), np.log(1e5), nprob))).astype(np.int64)
+        Mt = int(Ms.sum())
+        xy = ((torch.rand(2, Mt, generator=g, device="cuda", dtype=torch.float64) * 2 - 1)
+              * np.pi).to(torch.float32)
+        c = torch.randn(Mt, 2, generator=g, device="cuda").view(torch.complex64)[:, 0]
+        nm = np.concatenate([Ns, np.ones((nprob, 1), np.int64)], axis=1).ravel()
+        lib = fg.load_library()
+        plan = ctypes.c_void_p()
+        from finufft_gb300 import _lib
+
+        o = _lib.default_opts()
+        o.gpu_stream = stream.cuda_stream
+        assert lib.cufinufftf_batch_makeplan(1, 2, nprob, nm.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_int64)), 1, 1e-6, ctypes.byref(plan), ctypes.byref(o), None) == 0
+        t0 = time.perf_counter()
+        assert lib.cufinufftf_batch_setpts(plan, Ms.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                           xy[0].data_ptr(), xy[1].data_ptr(), None) == 0
+        torch.cuda.synchronize()
+        setpts_s = time.perf_counter() - t0
+        fk = torch.empty(int((Ns[:, 0] * Ns[:, 1]).sum()), dtype=torch.complex64, device=dev)
+        ms = _timed(lambda: lib.cufinufftf_batch_execute(plan, c.data_ptr(), fk.data_ptr()),
+                    stream, args.steps, args.warmup)
+        lib.cufinufftf_batch_destroy(plan)
+        # per-problem times: a sample of problems run alone through single plans
+        per = []
+        off = np.concatenate([[0], np.cumsum(Ms)])
+        for pidx in rng.choice(nprob, size=min(256, nprob), replace=False):
+            a, b = off[pidx], off[pidx + 1]
+            sp = fg.Plan(1, (int(Ns[pidx, 1]), int(Ns[pidx, 0])), eps=1e-6,
+                         gpu_stream=stream.cuda_stream)
+            sp.setpts(xy[1, a:b].contiguous(), xy[0, a:b].contiguous())
+            cc = c[a:b].contiguous()
+            per.append(_timed(lambda: sp.execute(cc), stream, 3, 1))
+        out.update({"workload": "4096 uneven 2D type 1 FP32, N/side log-uniform [32,256], M "
+                                "log-uniform [1e3,1e5], tol 1e-6, one batched plan",
+                    "value": Mt / (ms * 1e-3), "unit": "NU pts/s", "ms_per_step": ms,
+                    "M_total": Mt, "setpts_s": setpts_s,
+                    "per_problem_ms_single_plans": {"p50": float(np.percentile(per, 50)),
+                                                    "p99": float(np.percentile(per, 99)),
+                                                    "sample": len(per)},
+                    "batched_ms_per_problem": ms / nprob})
+    elif args.config == "c5":
+        # 3D type 3: M = K = 1e7, sources in box (1,2,4), targets in box (200,100,50)
+        M = K = 10_000_000
+        hs = torch.tensor([1.0, 2.0, 4.0], device="cuda", dtype=torch.float64)[:, None]
+        ht = torch.tensor([200.0, 100.0, 50.0], device="cuda", dtype=torch.float64)[:, None]
+        xs = ((torch.rand(3, M, generator=g, device="cuda", dtype=torch.float64) * 2 - 1) * hs).to(torch.float32)
+        ss = ((torch.rand(3, K, generator=g, device="cuda", dtype=torch.float64) * 2 - 1) * ht).to(torch.float32)
+        c = torch.randn(M, 2, generator=g, device="cuda").view(torch.complex64)[:, 0]
+        p = fg.Plan(3, 3, eps=1e-6, gpu_stream=stream.cuda_stream)
+        p.setpts(xs[0], xs[1], xs[2], s=ss[0], t=ss[1], u=ss[2])
+        f = torch.empty(K, dtype=torch.complex64, device=dev)
+        ms = _timed(lambda: p.execute(c, out=f), stream, args.steps, args.warmup)
+        # error on 256 sampled targets against an FP64 direct sum
+        nchk, blk = 256, 500_000
+        idx = torch.randint(0, K, (nchk,), generator=g, device="cuda")
+        S = ss[:, idx].to(torch.float64)
+        X = xs.to(torch.float64)
+        ref = torch.zeros(nchk, dtype=torch.complex128, device=dev)
+        for j0 in range(0, M, blk):
+            ph = S.T @ X[:, j0:j0 + blk]
+            ref += (torch.polar(torch.ones_like(ph), ph) * c[j0:j0 + blk].to(torch.complex128)).sum(1)
+        err = float(torch.linalg.norm(f[idx].to(torch.complex128) - ref) / torch.linalg.norm(ref))
+        info = p.info()
+        out.update({"workload": "3D type 3 FP32, M=K=1e7, boxes (1,2,4) x (200,100,50), tol 1e-6",
+                    "value": (M + K) / (ms * 1e-3), "unit": "NU pts/s (M+K)", "ms_per_step": ms,
+                    "rel_l2_err_sampled": err, "upsampfac": info.upsampfac, "ns": info.ns,
+                    "nf": list(info.nf), "inner_nf": list(info.inner_nf)})
+    print(json.dumps(out))
+
+
 def run_reference(args):
     """CPU FINUFFT restatement on the host cores, same metric and config."""
     rank, world, local = dist_info()
@@ -341,6 +476,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4_000_000)
     ap.add_argument("--err-modes", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="c3 (default) is the metric line; the others print their own line")
     ap.add_argument("--nmodes", type=int, default=0, help="modes per side (profiling cases)")
     ap.add_argument("--variant", type=int, default=-1, help="3D spread variant (tuning runs)")
     ap.add_argument("--planner", type=int, default=0, help="1: reference heuristic planning")
@@ -349,6 +486,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config != "c3":
+        run_config(args)
     else:
         run_gpu(args)
 

@@ -474,7 +474,9 @@ template <typename T> void Plan<T>::execute(cplx<T> *c, cplx<T> *fk) {
   else if (type == 2) run_type2(fk, c, ntransf, iflag, nullptr, 0);
   else {
     // type 3: pre-phase+spread onto the outer grid, inner type 2, post factor
+    // (stage timing: total only)
     const PointLayout<T> L = layout();
+    if (time_stages) GBN_CUDA(cudaEventRecord(ev[0], stream));
     for (int i = 0; i * batchsize < ntransf; ++i) {
       const int blk = std::min(ntransf - i * batchsize, batchsize);
       const cplx<T> *cb = c + (int64_t)i * batchsize * M;
@@ -484,14 +486,23 @@ template <typename T> void Plan<T>::execute(cplx<T> *c, cplx<T> *fk) {
                        stream);
       inner->run_type2(fw.p, fb, blk, iflag, t3post.p, 0);
     }
+    if (time_stages) {
+      GBN_CUDA(cudaEventRecord(ev[3], stream));
+      for (int k = 1; k < 3; ++k) GBN_CUDA(cudaEventRecord(ev[k], stream));
+    }
   }
   GBN_LAUNCH_CHECK();
   if (time_stages) {
+    // events: ev0 | spread or amplify | ev1 | FFT | ev2 | deconvolve or interp | ev3
     GBN_CUDA(cudaEventSynchronize(ev[3]));
-    cudaEventElapsedTime(&times.spread_or_interp_ms, ev[0], ev[1]);
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, ev[0], ev[1]);
     cudaEventElapsedTime(&times.fft_ms, ev[1], ev[2]);
-    cudaEventElapsedTime(&times.deconv_ms, ev[2], ev[3]);
+    cudaEventElapsedTime(&b, ev[2], ev[3]);
     cudaEventElapsedTime(&times.total_ms, ev[0], ev[3]);
+    times.spread_or_interp_ms = type == 2 ? b : a;
+    times.deconv_ms = type == 2 ? a : b;
+    if (type == 3) times.spread_or_interp_ms = times.fft_ms = times.deconv_ms = 0;
   }
 }
 

@@ -57,6 +57,7 @@ GBNUFFT_EXPORT void gbnufft_default_opts(gbnufft_opts *o);
   GBNUFFT_EXPORT int P##_plan_info(PLAN plan, gbnufft_plan_info *info);                  \
   /* enable != 0 turns on CUDA-event timing of the stages of later executes;        */  \
   /* ms[0..3] = spread-or-interp, FFT, deconvolve-or-amplify, total of the last one */  \
+  /* (type 3: total only, the other three are 0)                                    */  \
   GBNUFFT_EXPORT int P##_stage_times(PLAN plan, int enable, float ms[4]);                \
   /* Copies the device bin sort to host arrays: perm[M] (sorted position -> input   */  \
   /* index) and loc[dim*M] (bin-local coordinates, dimension-major).                */  \
