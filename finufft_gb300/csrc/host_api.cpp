@@ -39,8 +39,16 @@ template <typename T> struct HostPlan {
   int64_t M = 0, N = 0, nmodes = 1;
   DevArray<T> xyz[3], stu[3];
   DevArray<gbn::cplx<T>> dc, dfk;
+  // copy streams and events of the pipelined execute (input copy of batch k+1
+  // and output copy of batch k-1 overlap the transform of batch k)
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_done = nullptr;
   ~HostPlan() {
     plan.reset();
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_done) cudaEventDestroy(ev_done);
+    if (copy_in) cudaStreamDestroy(copy_in);
+    if (copy_out) cudaStreamDestroy(copy_out);
     for (auto &a : xyz) a.release();
     for (auto &a : stu) a.release();
     dc.release();
@@ -80,7 +88,10 @@ int makeplan_host(int type, int dim, const int64_t *n_modes, int iflag, int ntr,
     co.gpu_spreadinterponly = fo.spreadinterponly;
     co.debug = fo.debug;
     co.upsampfac = fo.upsampfac;
-    co.gpu_maxbatchsize = fo.maxbatchsize;
+    // batches of the pipelined execute: at least four when ntr allows, at most 8
+    // transforms each, so that copies of one batch overlap the next
+    co.gpu_maxbatchsize = fo.maxbatchsize > 0 ? fo.maxbatchsize
+                                              : std::min(8, std::max(1, (ntr + 3) / 4));
     if (fo.spread_max_sp_size > 0) co.gpu_maxsubprobsize = fo.spread_max_sp_size;
     // the CPU library accepts any sigma > 1: use direct kernel evaluation off the
     // two sigmas the GPU interface reserves for its Horner option
@@ -91,6 +102,10 @@ int makeplan_host(int type, int dim, const int64_t *n_modes, int iflag, int ntr,
     co.gpu_device_id = dev;
     auto h = std::make_unique<HostPlan<T>>();
     GBN_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    GBN_CUDA(cudaStreamCreateWithFlags(&h->copy_in, cudaStreamNonBlocking));
+    GBN_CUDA(cudaStreamCreateWithFlags(&h->copy_out, cudaStreamNonBlocking));
+    GBN_CUDA(cudaEventCreateWithFlags(&h->ev_in, cudaEventDisableTiming));
+    GBN_CUDA(cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming));
     co.gpu_stream = h->stream;
     h->type = type;
     h->dim = dim;
@@ -143,26 +158,47 @@ int setpts_host(void *p, int64_t M, const T *x, const T *y, const T *z, int64_t 
   });
 }
 
-// c: weights at the sources (M per transform); f: modes (type 1, 2) or target values (type 3)
+// c: weights at the sources (M per transform); f: modes (type 1, 2) or target values (type 3).
+// The transforms run in the plan's batches, pipelined over three streams: the
+// input copy of batch k+1 and the output copy of batch k-1 overlap batch k (with
+// pinned host arrays the copies are asynchronous DMA; with pageable arrays the
+// driver stages them and the overlap is partial).
 template <typename T>
 int execute_host(void *p, std::complex<T> *c, std::complex<T> *f, bool adjoint) {
   return guarded([&] {
     HostPlan<T> *h = hp<T>(p);
-    const int64_t nc = h->M * h->ntr;
-    const int64_t nf = (h->type == 3 ? h->N : h->nmodes) * h->ntr;
+    const int64_t per_c = h->M;
+    const int64_t per_f = h->type == 3 ? h->N : h->nmodes;
     // which side is input: type 1/3 forward and type 2 adjoint read c
     const bool c_in = (h->type != 2) != adjoint;
-    const size_t bc = (size_t)nc * sizeof(std::complex<T>), bf = (size_t)nf * sizeof(std::complex<T>);
-    if (c_in) {
-      if (bc) GBN_CUDA(cudaMemcpyAsync(h->dc.p, c, bc, cudaMemcpyHostToDevice, h->stream));
-    } else if (bf)
-      GBN_CUDA(cudaMemcpyAsync(h->dfk.p, f, bf, cudaMemcpyHostToDevice, h->stream));
-    if (adjoint) h->plan->execute_adjoint(h->dc.p, h->dfk.p);
-    else h->plan->execute(h->dc.p, h->dfk.p);
-    if (c_in) {
-      if (bf) GBN_CUDA(cudaMemcpyAsync(f, h->dfk.p, bf, cudaMemcpyDeviceToHost, h->stream));
-    } else if (bc)
-      GBN_CUDA(cudaMemcpyAsync(c, h->dc.p, bc, cudaMemcpyDeviceToHost, h->stream));
+    const int64_t per_in = c_in ? per_c : per_f, per_out = c_in ? per_f : per_c;
+    gbn::cplx<T> *din = c_in ? h->dc.p : h->dfk.p, *dout = c_in ? h->dfk.p : h->dc.p;
+    std::complex<T> *hin = c_in ? c : f, *hout = c_in ? f : c;
+    const size_t esz = sizeof(std::complex<T>);
+    const int bs = std::max(1, h->plan->batchsize);
+    const int nb = (h->ntr + bs - 1) / bs;
+    auto copy_in = [&](int b) {
+      const int t0 = b * bs, nt = std::min(bs, h->ntr - t0);
+      const size_t bytes = (size_t)nt * per_in * esz;
+      if (bytes)
+        GBN_CUDA(cudaMemcpyAsync(din + (int64_t)t0 * per_in, hin + (int64_t)t0 * per_in, bytes,
+                                 cudaMemcpyHostToDevice, h->copy_in));
+      GBN_CUDA(cudaEventRecord(h->ev_in, h->copy_in));
+    };
+    copy_in(0);
+    for (int b = 0; b < nb; ++b) {
+      const int t0 = b * bs, nt = std::min(bs, h->ntr - t0);
+      GBN_CUDA(cudaStreamWaitEvent(h->stream, h->ev_in, 0));
+      h->plan->execute_range(h->dc.p, h->dfk.p, t0, nt, adjoint);
+      GBN_CUDA(cudaEventRecord(h->ev_done, h->stream));
+      if (b + 1 < nb) copy_in(b + 1);
+      GBN_CUDA(cudaStreamWaitEvent(h->copy_out, h->ev_done, 0));
+      const size_t bytes = (size_t)nt * per_out * esz;
+      if (bytes)
+        GBN_CUDA(cudaMemcpyAsync(hout + (int64_t)t0 * per_out, dout + (int64_t)t0 * per_out,
+                                 bytes, cudaMemcpyDeviceToHost, h->copy_out));
+    }
+    GBN_CUDA(cudaStreamSynchronize(h->copy_out));
     GBN_CUDA(cudaStreamSynchronize(h->stream));
   });
 }

@@ -465,34 +465,68 @@ void Plan<T>::run_type2(const cplx<T> *fk, cplx<T> *c, int ntr, int sign,
 }
 
 template <typename T> void Plan<T>::execute(cplx<T> *c, cplx<T> *fk) {
+  execute_range(c, fk, 0, ntransf, false);
+}
+
+// Adjoint of the planned transform (reference CPU semantics,
+// include/finufft/execute.hpp:318-357): type 1 -> type 2 with the opposite
+// sign (fk in, c out), type 2 -> type 1 with the opposite sign (c in, fk out),
+// type 3 -> the planned factors applied backwards and conjugated.
+template <typename T> void Plan<T>::execute_adjoint(cplx<T> *c, cplx<T> *fk) {
+  execute_range(c, fk, 0, ntransf, true);
+}
+
+// Transforms [t0, t0 + nt) of the planned ntransf; c and fk point at the full
+// arrays (transform t at c + t*M, fk + t*(modes or targets)).
+template <typename T>
+void Plan<T>::execute_range(cplx<T> *c, cplx<T> *fk, int t0, int nt, bool adjoint) {
   DeviceScope ds(opts.gpu_device_id);
   check_ready();
-  if (time_stages)
+  if (t0 < 0 || nt < 0 || t0 + nt > ntransf)
+    GBN_THROW(FINUFFT_ERR_NTRANS_NOTVALID, "transform range");
+  if (nt == 0) return;
+  c += (int64_t)t0 * M;
+  fk += (int64_t)t0 * (type == 3 ? (int64_t)N : nmodes);
+  const bool timed = time_stages && !adjoint;
+  const bool tmp_ts = time_stages;
+  time_stages = timed;
+  if (timed)
     for (auto &e : ev)
       if (!e) GBN_CUDA(cudaEventCreate(&e));
-  if (type == 1) run_type1(c, fk, ntransf, iflag, nullptr, 0);
-  else if (type == 2) run_type2(fk, c, ntransf, iflag, nullptr, 0);
-  else {
-    // type 3: pre-phase+spread onto the outer grid, inner type 2, post factor
-    // (stage timing: total only)
-    const PointLayout<T> L = layout();
-    if (time_stages) GBN_CUDA(cudaEventRecord(ev[0], stream));
-    for (int i = 0; i * batchsize < ntransf; ++i) {
-      const int blk = std::min(ntransf - i * batchsize, batchsize);
-      const cplx<T> *cb = c + (int64_t)i * batchsize * M;
-      cplx<T> *fb = fk + (int64_t)i * batchsize * N;
-      GBN_CUDA(cudaMemsetAsync(fw.p, 0, (size_t)blk * nf_total * sizeof(cplx<T>), stream));
-      launch_spread<T>(L, K, cb, t3pre.p ? t3pre.p : nullptr, 0, fw.p, nf_total, blk, scfg,
-                       stream);
-      inner->run_type2(fw.p, fb, blk, iflag, t3post.p, 0);
-    }
-    if (time_stages) {
-      GBN_CUDA(cudaEventRecord(ev[3], stream));
-      for (int k = 1; k < 3; ++k) GBN_CUDA(cudaEventRecord(ev[k], stream));
-    }
+  if (!adjoint) {
+    if (type == 1) run_type1(c, fk, nt, iflag, nullptr, 0);
+    else if (type == 2) run_type2(fk, c, nt, iflag, nullptr, 0);
+  } else {
+    if (type == 1) run_type2(fk, c, nt, -iflag, nullptr, 0);
+    else if (type == 2) run_type1(c, fk, nt, -iflag, nullptr, 0);
   }
+  if (type == 3) {
+    const PointLayout<T> L = layout();
+    if (timed) GBN_CUDA(cudaEventRecord(ev[0], stream));
+    for (int i = 0; i * batchsize < nt; ++i) {
+      const int blk = std::min(nt - i * batchsize, batchsize);
+      cplx<T> *cb = c + (int64_t)i * batchsize * M;
+      cplx<T> *fb = fk + (int64_t)i * batchsize * N;
+      if (!adjoint) {
+        // pre-phase+spread onto the outer grid, inner type 2, post factor
+        GBN_CUDA(cudaMemsetAsync(fw.p, 0, (size_t)blk * nf_total * sizeof(cplx<T>), stream));
+        launch_spread<T>(L, K, cb, t3pre.p ? t3pre.p : nullptr, 0, fw.p, nf_total, blk, scfg,
+                         stream);
+        inner->run_type2(fw.p, fb, blk, iflag, t3post.p, 0);
+      } else {
+        // adjoint of (post * inner type 2): inner type 1 with conj(post) pre-factor,
+        // then the adjoint of (spread * pre): interpolate, times conj(pre)
+        inner->run_type1(fb, fw.p, blk, -iflag, t3post.p, 1);
+        launch_interp<T>(L, K, fw.p, nf_total, t3pre.p ? t3pre.p : nullptr, 1, cb, blk,
+                         stream);
+      }
+    }
+    if (timed) // stage timing of type 3: total only
+      for (int k = 3; k >= 1; --k) GBN_CUDA(cudaEventRecord(ev[k], stream));
+  }
+  time_stages = tmp_ts;
   GBN_LAUNCH_CHECK();
-  if (time_stages) {
+  if (timed) {
     // events: ev0 | spread or amplify | ev1 | FFT | ev2 | deconvolve or interp | ev3
     GBN_CUDA(cudaEventSynchronize(ev[3]));
     float a = 0, b = 0;
@@ -504,33 +538,6 @@ template <typename T> void Plan<T>::execute(cplx<T> *c, cplx<T> *fk) {
     times.deconv_ms = type == 2 ? a : b;
     if (type == 3) times.spread_or_interp_ms = times.fft_ms = times.deconv_ms = 0;
   }
-}
-
-// Adjoint of the planned transform (reference CPU semantics,
-// include/finufft/execute.hpp:318-357): type 1 -> type 2 with the opposite
-// sign (fk in, c out), type 2 -> type 1 with the opposite sign (c in, fk out),
-// type 3 -> the planned factors applied backwards and conjugated.
-template <typename T> void Plan<T>::execute_adjoint(cplx<T> *c, cplx<T> *fk) {
-  DeviceScope ds(opts.gpu_device_id);
-  check_ready();
-  const bool tmp_ts = time_stages;
-  time_stages = false;
-  if (type == 1) run_type2(fk, c, ntransf, -iflag, nullptr, 0);
-  else if (type == 2) run_type1(c, fk, ntransf, -iflag, nullptr, 0);
-  else {
-    const PointLayout<T> L = layout();
-    for (int i = 0; i * batchsize < ntransf; ++i) {
-      const int blk = std::min(ntransf - i * batchsize, batchsize);
-      cplx<T> *cb = c + (int64_t)i * batchsize * M;
-      const cplx<T> *fb = fk + (int64_t)i * batchsize * N;
-      // adjoint of (post * inner type 2): inner type 1 with conj(post) pre-factor
-      inner->run_type1(fb, fw.p, blk, -iflag, t3post.p, 1);
-      // adjoint of (spread * pre): interpolate, times conj(pre)
-      launch_interp<T>(L, K, fw.p, nf_total, t3pre.p ? t3pre.p : nullptr, 1, cb, blk, stream);
-    }
-  }
-  time_stages = tmp_ts;
-  GBN_LAUNCH_CHECK();
 }
 
 template class Plan<float>;

@@ -70,6 +70,8 @@ public:
               const T *t, const T *u);
   void execute(cplx<T> *c, cplx<T> *fk);
   void execute_adjoint(cplx<T> *c, cplx<T> *fk);
+  // transforms [t0, t0 + nt) only (c, fk: the full arrays)
+  void execute_range(cplx<T> *c, cplx<T> *fk, int t0, int nt, bool adjoint);
 
   // introspection (tests, planner, benchmarks)
   int type, dim, ntransf, iflag, batchsize;

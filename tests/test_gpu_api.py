@@ -196,6 +196,56 @@ def test_host_pointer_api(oracle, engine, prec):
     assert getattr(engine, pfx + "_destroy")(p) == 0
 
 
+@pytest.mark.parametrize("ty", [1, 2, 3])
+def test_host_pointer_pipelined_batches(oracle, engine, ty):
+    """Host-pointer execute over several batches (input copy of batch k+1 and
+    output copy of batch k-1 overlap batch k): 5 transforms in batches of 2,
+    from pinned and from pageable host arrays, each equal to a direct sum."""
+    import torch
+
+    from finufft_gb300 import _lib
+
+    rng = np.random.default_rng(40 + ty)
+    M, nm, ntr, tol = 2500, (12, 10, 8), 5, 1e-5
+    x, y, z = rng.uniform(-np.pi, np.pi, (3, M)).astype(np.float32)
+    o = _lib.FinufftOpts()
+    engine.finufft_default_opts(ctypes.byref(o))
+    o.maxbatchsize = 2
+    p = ctypes.c_void_p()
+    m = (ctypes.c_int64 * 3)(*nm)
+    assert engine.finufftf_makeplan(ty, 3, m, 1 if ty != 2 else -1, ntr, tol, ctypes.byref(p),
+                                    ctypes.byref(o)) == 0
+    K = 700
+    s, t, u = (rng.uniform(-9, 9, (3, K)).astype(np.float32) if ty == 3 else (None,) * 3)
+    ptr = (lambda a: a.ctypes.data if a is not None else None)
+    assert engine.finufftf_setpts(p, M, x.ctypes.data, y.ctypes.data, z.ctypes.data,
+                                  K if ty == 3 else 0, ptr(s), ptr(t), ptr(u)) == 0
+    nout = K if ty == 3 else int(np.prod(nm))
+    for pinned in (True, False):
+        if ty == 2:
+            fin = _cx(rng, (ntr, int(np.prod(nm))))
+            cout = torch.zeros(ntr * M, dtype=torch.complex64, pin_memory=pinned).numpy()
+            fh = torch.from_numpy(fin.ravel().copy())
+            fh = fh.pin_memory() if pinned else fh
+            assert engine.finufftf_execute(p, cout.ctypes.data, fh.numpy().ctypes.data) == 0
+            for k in range(ntr):
+                ref = oracle.dirft2([x, y, z], fin[k], -1, nm)
+                assert oracle.rel_l2(cout[k * M:(k + 1) * M], ref) < 20 * tol
+        else:
+            cin = _cx(rng, (ntr, M))
+            ch = torch.from_numpy(cin.ravel().copy())
+            ch = ch.pin_memory() if pinned else ch
+            fout = torch.zeros(ntr * nout, dtype=torch.complex64, pin_memory=pinned).numpy()
+            assert engine.finufftf_execute(p, ch.numpy().ctypes.data, fout.ctypes.data) == 0
+            for k in range(ntr):
+                if ty == 1:
+                    ref = oracle.dirft1([x, y, z], cin[k], 1, nm)
+                else:
+                    ref = oracle.dirft3([x, y, z], cin[k], 1, [s, t, u])
+                assert oracle.rel_l2(fout[k * nout:(k + 1) * nout], ref) < 20 * tol
+    assert engine.finufftf_destroy(p) == 0
+
+
 def test_simple_interfaces(oracle, engine):
     import torch
 
