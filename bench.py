@@ -143,6 +143,11 @@ def run_gpu(args):
         plan_kw["spread_variant"] = args.variant
     if args.planner:
         plan_kw["planner"] = args.planner
+    if args.bins:
+        bx, by, bz = (int(v) for v in args.bins.split(","))
+        plan_kw.update(gpu_binsizex=bx, gpu_binsizey=by, gpu_binsizez=bz)
+    if args.maxsub:
+        plan_kw["gpu_maxsubprobsize"] = args.maxsub
     if world > 1:
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
@@ -194,6 +199,7 @@ def run_gpu(args):
     bplan.execute(c, out=fkb)
     torch.cuda.synchronize()
     stb = bplan.stage_times(True)
+    binfo = bplan.info()
 
     # e2e through the reference-facing host-pointer C ABI (finufftf_makeplan /
     # setpts / execute) with pinned host arrays: every step copies the nt strength
@@ -239,6 +245,14 @@ def run_gpu(args):
     spread_ms = stb[0]
     achieved = atom_per_launch / (spread_ms * 1e-3)
     peak = fg.smem_atomic_peak(dev.index) if hasattr(fg, "smem_atomic_peak") else None
+    kname = {0: "spread_tile3_kernel", 1: "spread_tile3w_kernel", 2: "spread_tile3m_kernel",
+             3: "spread_tile3v_kernel"}.get(binfo.spread_variant, "spread_global_kernel")
+    # algorithmic HBM bytes of one spread launch (nt transforms): coordinates and
+    # strengths read once (3*4 + 2*4 B per point per transform), fine grid written
+    nf_cells = int(np.prod(list(binfo.nf)))
+    hbm_bytes = float(M) * (12 + 8 * nt) + nf_cells * 8.0 * nt
+    hbm_ach = hbm_bytes / (spread_ms * 1e-3)
+    hbm_peak = measured_peak("hbm_gbs")
 
     tot_ms = torch.tensor([ms_batched, ms_plain, ms_e2e], dtype=torch.float64, device=dev)
     if world > 1:
@@ -270,8 +284,14 @@ def run_gpu(args):
         "gpu_launches": 2 * args.steps,
         "roofline": {"bound": "smem_atomic", "achieved": achieved / 1e9,
                      "peak": (peak / 1e9) if peak else None, "unit": "G atomic f32 adds/s",
-                     "frac": (achieved / peak) if peak else None, "traffic": None,
-                     "kernel": "spread_tile_kernel", "per_launch": atom_per_launch},
+                     "frac": (achieved / peak) if peak else None, "traffic": SPREAD_TRAFFIC,
+                     "kernel": kname, "per_launch": atom_per_launch,
+                     "peak_source": "measured by gbnufft_smem_atomic_rate on this GPU"},
+        "roofline_hbm": {"bound": "hbm", "achieved": hbm_ach / 1e9, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": (hbm_ach / 1e9 / hbm_peak) if hbm_peak else None,
+                         "traffic": SPREAD_TRAFFIC, "kernel": kname,
+                         "algorithmic_bytes_per_launch": hbm_bytes,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "clocks": clk.summary(),
     }
     if not args.no_cpu and world == 1:
@@ -279,6 +299,20 @@ def run_gpu(args):
     print(json.dumps(out))
     if world > 1:
         dist.barrier()
+
+
+# DRAM bytes (read + write) of one spread launch from an ncu capture, scaled to
+# this workload; None until a capture of the default kernel is recorded
+SPREAD_TRAFFIC = None
+
+
+def measured_peak(key):
+    """a peak from MEASURED_PEAKS.json at the repository root (None if absent)"""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)[key])
+    except (OSError, KeyError, ValueError):
+        return None
 
 
 def sampled_error(x, y, z, c, fk, dev, nsample=64, seed=5):
@@ -501,6 +535,8 @@ def main():
     ap.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c3 (default) is the metric line; the others print their own line")
     ap.add_argument("--nmodes", type=int, default=0, help="modes per side (profiling cases)")
+    ap.add_argument("--bins", default="", help="bin sizes x,y,z (default: the planner's)")
+    ap.add_argument("--maxsub", type=int, default=0, help="max points per subproblem")
     ap.add_argument("--variant", type=int, default=-1, help="3D spread variant (tuning runs)")
     ap.add_argument("--planner", type=int, default=0, help="1: reference heuristic planning")
     ap.add_argument("--only", default="", choices=["", "plain"],

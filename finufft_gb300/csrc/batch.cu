@@ -407,6 +407,7 @@ template <typename T> PointLayout<T> BatchPlan<T>::layout() const {
   L.perm = perm.p;
   L.probs = d_bprob.p;
   L.binprob = binprob.p;
+  L.cell_sorted = 1;
   return L;
 }
 

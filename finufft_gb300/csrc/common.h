@@ -90,6 +90,8 @@ template <typename T> struct PointLayout {
   // problems, whose grids and bin counts replace nf/nbin above (null otherwise)
   const BatchProb *probs = nullptr;
   const int *binprob = nullptr;
+  // 1 when points inside a bin are also sorted by cell (x fastest, z slowest)
+  int cell_sorted = 0;
 };
 
 } // namespace gbn

@@ -32,6 +32,12 @@ template <typename T> size_t spread_tile3m_bytes(int ns, const int bin[3], int w
   return tile3_bytes<T>(ns, bin[0], bin[1], bin[2]) +
          (size_t)warps * t3m_stage_bytes(ns, (int)sizeof(T));
 }
+template <typename T> size_t spread_tile3v_bytes(int ns, const int bin[3], int warps) {
+  return tile3v_bytes<T>(ns, bin[0], bin[1], bin[2]) +
+         (size_t)warps * t3v_stage_bytes(ns, (int)sizeof(T));
+}
+template size_t spread_tile3v_bytes<float>(int, const int[3], int);
+template size_t spread_tile3v_bytes<double>(int, const int[3], int);
 template <typename T> size_t spread_tile2m_bytes(int ns, const int bin[3]) {
   const size_t tile = (2 * sizeof(T) * (size_t)tile_pitch_x(3, bin[0] + ns) * (bin[1] + ns) + 15) /
                       16 * 16;

@@ -139,6 +139,7 @@ int spread_noalloc_f(int dim, const int64_t *n_grid, int64_t M, const float *x, 
     L.sub_start = sa.start;
     L.sub_count = sa.count;
     L.perm = perm;
+    L.cell_sorted = cell_keys;
     launch_spread<float>(L, K, c, nullptr, 0, grid, cells, 1, S.cfg, stream);
     GBN_CUDA(cudaGetLastError());
     return 0;

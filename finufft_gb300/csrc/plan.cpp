@@ -13,6 +13,7 @@
 
 #include "planning.h"
 #include "sort.h"
+#include "tile_layout.h"
 
 extern "C" void gbnufft_default_opts(gbnufft_opts *o) {
   if (!o) return;
@@ -182,15 +183,41 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
   }
   if (dim == 3 && S.method == 2) {
     // 3D tiled variants: 0 shared tile + per-point atomics, 1 exclusive-warp tiles,
-    // 2 shared tile + per-run (warp-aggregated) atomics; default 2
+    // 2 shared tile + per-run (warp-aggregated) atomics, 3 as 2 with x-slack runs
+    // and vector staging
     const size_t wsm = spread_tile3w_bytes<T>(ns, bins);
     // per-run register accumulators cost 2*ceil(ns/8)*ceil(ns^2/4) registers, so
     // the warp-aggregated variant is used for ns <= 8 only
-    int variant = ext.planner == 1 ? 0 : (ns <= 8 ? 2 : 0);
+    // default: 3 where its accumulators fit the register budget without spills
+    // (single precision ns <= 8, double ns <= 5), else 2 for ns <= 8, else 0
+    const bool v3ok = std::is_same_v<T, float> ? ns <= 8 : ns <= 5;
+    int variant = ext.planner == 1 ? 0 : (v3ok ? 3 : (ns <= 8 ? 2 : 0));
     if (ext.spread_variant >= 0) variant = ext.spread_variant;
     if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT")) variant = std::atoi(e);
     if (variant == 1 && wsm > (size_t)limit) variant = 2;
-    if (variant < 0 || variant > 2 || (variant == 2 && ns > 8)) variant = 0;
+    if (variant < 0 || variant > 3 || (variant >= 2 && ns > 8)) variant = 0;
+    if (variant == 3) {
+      // 3: variant 2 with x-slack runs and vector staging; the most warps (within
+      // the kernel's launch bound) that keep two blocks per SM, else that fit one
+      const int half = 113 * 1024;
+      const int wmax = t3v_max_threads<T>() / 32;
+      int w = wmax;
+      while (w > 4 && spread_tile3v_bytes<T>(ns, bins, w) > (size_t)half) --w;
+      if (spread_tile3v_bytes<T>(ns, bins, w) > (size_t)half) {
+        w = wmax;
+        while (w > 1 && spread_tile3v_bytes<T>(ns, bins, w) > (size_t)limit) --w;
+      }
+      const size_t vsm = spread_tile3v_bytes<T>(ns, bins, w);
+      if (vsm > (size_t)limit) {
+        variant = 2;
+      } else {
+        S.cfg.variant = 3;
+        S.cfg.threads = 32 * w;
+        S.cfg.smem = vsm;
+        S.smem = vsm;
+        return S;
+      }
+    }
     const int mwarps = std::is_same_v<T, float> ? 12 : 8;
     const size_t msm = spread_tile3m_bytes<T>(ns, bins, mwarps);
     if (variant == 2 && msm > (size_t)limit) variant = 0;
@@ -264,6 +291,7 @@ template <typename T> PointLayout<T> Plan<T>::layout() const {
   L.sub_start = sub_start_.p;
   L.sub_count = sub_count_.p;
   L.perm = perm.p;
+  L.cell_sorted = cell_sorted;
   return L;
 }
 
@@ -276,6 +304,7 @@ void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]
   // keys carry the cell inside the bin when bins * bin volume fits 32 bits
   const uint64_t binvol = (uint64_t)bins[0] * bins[1] * bins[2];
   const int cell_keys = (uint64_t)nb * binvol <= 0xffffffffull ? 1 : 0;
+  cell_sorted = cell_keys;
   const uint64_t nkeys = cell_keys ? (uint64_t)nb * binvol : (uint64_t)nb;
   int keybits = 0;
   while ((1ull << keybits) < nkeys) ++keybits;

@@ -88,6 +88,7 @@ public:
   int bins[3] = {1, 1, 1};
   int nbins[3] = {1, 1, 1};
   int nsub = 0;
+  int cell_sorted = 0; // points sorted by (bin, cell in bin)
   size_t spread_smem = 0;
   cudaStream_t stream = nullptr;
   StageTimes times;

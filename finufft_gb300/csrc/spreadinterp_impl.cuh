@@ -496,6 +496,236 @@ __global__ void __launch_bounds__(t3m_threads<T>(), 2)
 }
 
 // ---------------------------------------------------------------------------
+// Method 2 in 3D, warp-aggregated with x slack and vector staging (variant 3,
+// ns <= 8). As spread_tile3m_kernel, but a register run also absorbs points
+// whose x start lies up to 8 - ns cells right of the run's first point (the
+// 8 x lanes then cover the shifted footprint; x weights are read from
+// zero-padded rows), each point's (y, z) products are staged so a lane reads
+// its share as 16-byte vectors, the next batch's points are fetched while the
+// current batch is summed, and with (bin, cell)-sorted points only the z planes
+// the subproblem can touch are cleared and written back.
+template <typename T> struct Vec16;
+template <> struct Vec16<float> {
+  using type = float4;
+};
+template <> struct Vec16<double> {
+  using type = double2;
+};
+
+template <typename T, int NS>
+__global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
+    spread_tile3v_kernel(PointLayout<T> L0, KernelShape<T> K, const cplx<T> *__restrict__ c,
+                         const cplx<T> *__restrict__ pre, int conj_pre,
+                         cplx<T> *__restrict__ fw, int64_t nf_total) {
+  using V = typename Vec16<T>::type;
+  constexpr int TS = (int)sizeof(T);
+  constexpr int VW = t3v_vw(TS), NR = t3v_nr(NS), NRV = t3v_nrv(NS, TS);
+  constexpr int LPS = t3v_lps(NS, TS), QS = t3v_qs(NS, TS);
+  constexpr int XS = t3v_xs(NS), KXR = t3v_kxr(NS), SK = STAGE_STRIDE;
+  constexpr int HDR = 4 * LPS; // header vector(s) of a point block
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int sub = blockIdx.x;
+  const int tr = blockIdx.y;
+  int b = L0.sub_bin[sub];
+  PointLayout<T> Lg;
+  const int64_t goff = resolve_problem<T>(L0, Lg, b);
+  const PointLayout<T> &L = Lg;
+  const int p0 = L.sub_start[sub];
+  const int np = L.sub_count[sub];
+  if (np <= 0) return;
+  const TileGeom<3> G = tile_of<T, 3, NS>(L, b);
+  const int px = tile_pitch_x(3, L.bin[0] + 8);
+  const int py = tile3_py(G.t[1], NS);
+  const int Q = px * py;
+  const size_t tile_bytes = tile3v_bytes<T>(NS, L.bin[0], L.bin[1], L.bin[2]);
+  T *re = reinterpret_cast<T *>(smem_raw);
+  T *im = re + Q * G.t[2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  unsigned char *stg = smem_raw + tile_bytes + (size_t)warp * t3v_stage_bytes(NS, TS);
+  T *kx = reinterpret_cast<T *>(stg); // x weights [KXR][SK], rows XS..XS+NS-1 live
+  V *pts = reinterpret_cast<V *>(stg + (KXR * SK * TS + 15) / 16 * 16); // [32][QS]
+  // z planes the subproblem can touch: start cells lie in [cell, cell + 1] and
+  // cell-sorted points are z-major inside a bin (loc may round up to cell + 1)
+  int zlo = 0, zhi = G.t[2] - 1;
+  if (L.cell_sorted) {
+    zlo = max(0, (int)floor(L.loc[2][p0]) - 1);
+    zhi = min(G.t[2] - 1, (int)floor(L.loc[2][p0 + np - 1]) + NS);
+  }
+  // contiguous share of the subproblem's points for this warp
+  const int per = (np + nwarp - 1) / nwarp;
+  const int w0 = min(np, warp * per), w1 = min(np, w0 + per);
+  const cplx<T> *ct = c + (int64_t)tr * L.M;
+  cplx<T> pv;
+  T pl0 = T(0), pl1 = T(0), pl2 = T(0);
+  pv.x = pv.y = T(0);
+  auto fetch = [&](int i) {
+    if (i < w1) {
+      const int p = p0 + i;
+      const int j = L.perm[p];
+      pv = ct[j];
+      if (pre) pv = cmul_opt<T>(pv, pre[j], conj_pre);
+      pl0 = L.loc[0][p];
+      pl1 = L.loc[1][p];
+      pl2 = L.loc[2][p];
+    }
+  };
+  fetch(w0 + lane);
+  {
+    uint4 *z4 = reinterpret_cast<uint4 *>(re + (size_t)zlo * Q);
+    uint4 *z4i = reinterpret_cast<uint4 *>(im + (size_t)zlo * Q);
+    const int n16 = (zhi - zlo + 1) * Q * TS / 16;
+    const uint4 zero = make_uint4(0, 0, 0, 0);
+    for (int i = threadIdx.x; i < n16; i += blockDim.x) {
+      z4[i] = zero;
+      z4i[i] = zero;
+    }
+#pragma unroll
+    for (int t = 0; t < KXR; ++t)
+      if (t < XS || t >= XS + NS) kx[t * SK + lane] = T(0);
+  }
+  __syncthreads();
+  const int lx = lane & 7, lp = lane >> 3;
+  int off[NR];
+  bool ok[NR];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const int pp = 4 * r + lp;
+    ok[r] = pp < NS * NS;
+    off[r] = (pp / NS) * Q + (pp % NS) * px + lx;
+  }
+  T ar[NR], ai[NR];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) ar[r] = ai[r] = T(0);
+  int cur = -1;
+  const T *kxl = kx + (lx + XS) * SK; // row lx - dx + XS is kxl - dx * SK
+  auto flush = [&]() {
+    const int rb = (cur >> 20) * Q + ((cur >> 10) & 1023) * px + (cur & 1023);
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+      if (ok[r]) {
+        atomicAdd(re + rb + off[r], ar[r]);
+        atomicAdd(im + rb + off[r], ai[r]);
+      }
+  };
+  for (int base = w0; base < w1; base += 32) {
+    if (base + lane < w1) {
+      T ka[NS], kb[NS], kc[NS];
+      const int sx = point_weights<T, NS>(pl0, L.bin[0], K, ka);
+      const int sy = point_weights<T, NS>(pl1, L.bin[1], K, kb);
+      const int sz = point_weights<T, NS>(pl2, L.bin[2], K, kc);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) kx[(XS + a) * SK + lane] = ka[a];
+      V *pb = pts + lane * QS;
+#pragma unroll
+      for (int l4 = 0; l4 < 4; ++l4)
+#pragma unroll
+        for (int v = 0; v < NRV; ++v) {
+          V w;
+          T *e = reinterpret_cast<T *>(&w);
+#pragma unroll
+          for (int u = 0; u < VW; ++u) {
+            const int r = v * VW + u, pp = 4 * r + l4;
+            e[u] = (r < NR && pp < NS * NS) ? kb[pp % NS] * kc[pp / NS] : T(0);
+          }
+          pb[l4 * LPS + v] = w;
+        }
+      const int spk = sx | (sy << 10) | (sz << 20);
+      V h;
+      T *he = reinterpret_cast<T *>(&h);
+      he[0] = pv.x;
+      he[1] = pv.y;
+      if constexpr (VW == 4) {
+        he[2] = __int_as_float(spk);
+        he[3] = T(0);
+        pb[HDR] = h;
+      } else {
+        pb[HDR] = h;
+        V h2;
+        T *h2e = reinterpret_cast<T *>(&h2);
+        h2e[0] = __longlong_as_double((long long)spk);
+        h2e[1] = T(0);
+        pb[HDR + 1] = h2;
+      }
+    }
+    fetch(base + 32 + lane); // next batch, in flight while this one is summed
+    __syncwarp();
+    const int cnt = min(32, w1 - base);
+    for (int q = 0; q < cnt; ++q) {
+      const V *pq = pts + q * QS;
+      const V h = pq[HDR];
+      const T *he = reinterpret_cast<const T *>(&h);
+      const T vr = he[0], vi = he[1];
+      int sp;
+      if constexpr (VW == 4) sp = __float_as_int(he[2]);
+      else sp = (int)__double_as_longlong(pq[HDR + 1].x);
+      int dx = (sp & 1023) - (cur & 1023);
+      if (((sp ^ cur) >> 10) != 0 || (unsigned)dx > (unsigned)XS) {
+        if (cur >= 0) flush();
+#pragma unroll
+        for (int r = 0; r < NR; ++r) ar[r] = ai[r] = T(0);
+        cur = sp;
+        dx = 0;
+      }
+      const T wx = kxl[q - dx * SK];
+      const T xr = vr * wx, xi = vi * wx;
+      const V *wl = pq + lp * LPS;
+#pragma unroll
+      for (int v = 0; v < NRV; ++v) {
+        const V w = wl[v];
+        const T *e = reinterpret_cast<const T *>(&w);
+#pragma unroll
+        for (int u = 0; u < VW; ++u) {
+          const int r = v * VW + u;
+          if (r < NR) {
+            ar[r] = fma(xr, e[u], ar[r]);
+            ai[r] = fma(xi, e[u], ai[r]);
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
+  if (cur >= 0) flush();
+  __syncthreads();
+  // write back planes zlo..zhi: lanes cover (x, row) pairs
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total + goff;
+  const int tx = G.t[0], ty = G.t[1], tz = G.t[2];
+  const bool fits = tx <= L.nf[0] && ty <= L.nf[1] && tz <= L.nf[2] && NS <= 2 * L.nf[0] &&
+                    NS <= 2 * L.nf[1] && NS <= 2 * L.nf[2];
+  int txp = 1;
+  while (txp < tx && txp < 32) txp <<= 1;
+  const int rows_per = blockDim.x / txp;
+  const int rows = ty * (zhi - zlo + 1);
+  const int64_t plane = (int64_t)L.nf[0] * L.nf[1];
+  for (int x0 = 0; x0 < tx; x0 += txp) {
+    const int x = x0 + (threadIdx.x & (txp - 1));
+    const int gx = fits ? wrap_once(G.org[0] + x, L.nf[0]) : wrap_idx(G.org[0] + x, L.nf[0]);
+    int r0 = threadIdx.x / txp;
+    int y = r0 % ty, z = zlo + r0 / ty;
+    const int dy = rows_per % ty, dz = rows_per / ty;
+    for (; r0 < rows; r0 += rows_per) {
+      if (x < tx) {
+        const int sidx = z * Q + y * px + x;
+        cplx<T> v;
+        v.x = re[sidx];
+        v.y = im[sidx];
+        if (v.x != T(0) || v.y != T(0)) {
+          const int gy = fits ? wrap_once(G.org[1] + y, L.nf[1]) : wrap_idx(G.org[1] + y, L.nf[1]);
+          const int gz = fits ? wrap_once(G.org[2] + z, L.nf[2]) : wrap_idx(G.org[2] + z, L.nf[2]);
+          atomic_add_cplx_global(fwt + gx + (int64_t)L.nf[0] * gy + plane * gz, v);
+        }
+      }
+      y += dy;
+      z += dz;
+      if (y >= ty) {
+        y -= ty;
+        ++z;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Method 2 in 3D, exclusive-warp variant: one warp per block owns its tile, so
 // the tile is updated with plain shared-memory read-modify-writes instead of
 // atomics. Points arrive sorted by (bin, cell inside the bin); the contributions
@@ -1047,6 +1277,14 @@ template <typename T, int DIM> struct Dispatch {
       spread_global_kernel<T, DIM, NS><<<grid, GLOBAL_SPREAD_THREADS, 0, s>>>(L, K, c, pre, conj_pre, fw,
                                                                     nf_total);
     } else if constexpr (DIM == 3) {
+      if (NS <= 8 && cfg.variant == 3) {
+        auto kv = spread_tile3v_kernel<T, (NS <= 8 ? NS : 8)>;
+        GBN_CUDA(cudaFuncSetAttribute(kv, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)cfg.smem));
+        kv<<<grid, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
+        GBN_LAUNCH_CHECK();
+        return;
+      }
       if (NS <= 8 && cfg.variant == 2) {
         auto km = spread_tile3m_kernel<T, (NS <= 8 ? NS : 8)>;
         GBN_CUDA(cudaFuncSetAttribute(km, cudaFuncAttributeMaxDynamicSharedMemorySize,

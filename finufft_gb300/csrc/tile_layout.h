@@ -40,4 +40,41 @@ __host__ __device__ constexpr int t3m_stage_bytes(int ns, int tsize) {
   return (33 * (ns + 4 * ((ns * ns + 3) / 4) + 2) * tsize + 33 * 4 + 15) / 16 * 16;
 }
 
+// Warp-aggregated 3D spread with x slack and vector staging (ns <= 8). A run of
+// points sharing their (y, z) start cells whose x starts lie within 8 - ns
+// cells of the run's first point is summed in registers over an 8-cell x
+// window. Per point, the (y, z) weight products a lane needs (pairs 4r + lane
+// row) are stored contiguously so a lane reads them as 16-byte vectors; the
+// last vectors of a point block hold its strength and packed start cells.
+//   vw: elements per 16-byte vector; nrv: vectors per lane row; lps: lane-row
+//   stride in vectors (the four rows read at once fall in distinct bank groups);
+//   qs: point stride in vectors (odd, so 8 points' stores hit distinct groups)
+__host__ __device__ constexpr int t3v_vw(int tsize) { return 16 / tsize; }
+__host__ __device__ constexpr int t3v_nr(int ns) { return (ns * ns + 3) / 4; }
+__host__ __device__ constexpr int t3v_nrv(int ns, int tsize) {
+  return (t3v_nr(ns) + t3v_vw(tsize) - 1) / t3v_vw(tsize);
+}
+__host__ __device__ constexpr int t3v_lps(int ns, int tsize) {
+  return t3v_nrv(ns, tsize) % 4 == 0 ? t3v_nrv(ns, tsize) + 1 : t3v_nrv(ns, tsize);
+}
+__host__ __device__ constexpr int t3v_hdr(int tsize) { return tsize == 4 ? 1 : 2; }
+__host__ __device__ constexpr int t3v_qs(int ns, int tsize) {
+  return (4 * t3v_lps(ns, tsize) + t3v_hdr(tsize)) | 1;
+}
+__host__ __device__ constexpr int t3v_xs(int ns) { return 8 - ns; }    // x slack of a run
+__host__ __device__ constexpr int t3v_kxr(int ns) { return 8 + t3v_xs(ns); } // x rows
+__host__ __device__ constexpr int t3v_stage_bytes(int ns, int tsize) {
+  return (t3v_kxr(ns) * 33 * tsize + 15) / 16 * 16 + 32 * t3v_qs(ns, tsize) * 16;
+}
+// threads per block of that kernel at most (its register budget assumes two
+// blocks per SM)
+template <typename T> __host__ __device__ constexpr int t3v_max_threads() {
+  return sizeof(T) == 4 ? 320 : 256;
+}
+template <typename T>
+__host__ __device__ constexpr size_t tile3v_bytes(int ns, int bx, int by, int bz) {
+  return (2 * sizeof(T) * (size_t)tile_pitch_x(3, bx + 8) * tile3_py(by + ns, ns) * (bz + ns) +
+          15) / 16 * 16;
+}
+
 } // namespace gbn

@@ -136,3 +136,61 @@ def test_sort_bit_exact(oracle, dtype, dim):
                                   loc_dtype=rdt)
     np.testing.assert_array_equal(perm, hperm)
     np.testing.assert_array_equal(loc.reshape(dim, M), hloc)
+
+
+def _clustered(rng, dim, M, rdt):
+    """half uniform, half in two tight clusters (long same-cell runs, dense bins)"""
+    u = rng.uniform(-np.pi, np.pi, (dim, M - M // 2))
+    cen = rng.uniform(-np.pi, np.pi, (2, dim, 1))
+    k = rng.integers(0, 2, M // 2)
+    cl = cen[k, :, 0].T + 0.05 * rng.standard_normal((dim, M // 2))
+    cl = np.remainder(cl + np.pi, 2 * np.pi) - np.pi
+    return np.concatenate([u, cl], axis=1).astype(rdt)
+
+
+@pytest.mark.parametrize("dtype,tol", [("complex64", 1e-5), ("complex64", 1e-3),
+                                       ("complex64", 3e-7), ("complex128", 1e-7)])
+@pytest.mark.parametrize("bins", [None, (12, 4, 8)])
+def test_spread_variants_3d(oracle, dtype, tol, bins):
+    """3D type 1 through every tiled spread variant (0 per-point atomics, 1
+    exclusive-warp tiles, 2 warp-aggregated runs, 3 runs with x slack): each
+    equals the FP64 direct sum, and all agree with variant 0 to rounding."""
+    import finufft_gb300 as fg
+
+    rdt = np.float32 if dtype == "complex64" else np.float64
+    rng = np.random.default_rng(77)
+    nm, M, ntr = (14, 18, 22), 6000, 3
+    pts = _clustered(rng, 3, M, rdt)
+    c = _cx(rng, (ntr, M), dtype)
+    kw = {} if bins is None else dict(gpu_binsizex=bins[0], gpu_binsizey=bins[1],
+                                      gpu_binsizez=bins[2])
+    outs = {}
+    for v in (0, 1, 2, 3):
+        plan = fg.Plan(1, nm, n_trans=ntr, eps=tol, dtype=dtype, isign=1, spread_variant=v, **kw)
+        plan.setpts(*[_dev(p) for p in pts])
+        outs[v] = plan.execute(_dev(c)).cpu().numpy()
+        outs[v, "used"] = plan.info().spread_variant
+    ref = oracle.dirft1(_oracle_pts(pts), c[1], 1, nm[::-1])
+    for v in (0, 1, 2, 3):
+        got = outs[v][1].ravel()
+        assert oracle.rel_l2(got, ref) < max(20 * tol, 1e-5), (v, outs[v, "used"])
+        if v:
+            assert oracle.rel_l2(outs[v], outs[0]) < (2e-5 if dtype == "complex64" else 1e-12), v
+    assert outs[3, "used"] == 3 or tol < 1e-6  # width 8 and below take variant 3
+
+
+@pytest.mark.parametrize("v", [2, 3])
+def test_spread_variants_type3(oracle, v):
+    """type 3 (spread with the pre-phase factor) through the warp-aggregated variants"""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(78)
+    M, K = 5000, 400
+    x = _clustered(rng, 3, M, np.float32)
+    s = rng.uniform(-12, 12, (3, K)).astype(np.float32)
+    c = _cx(rng, M, "complex64")
+    plan = fg.Plan(3, 3, eps=1e-5, dtype="complex64", isign=1, spread_variant=v)
+    plan.setpts(*[_dev(a) for a in x], s=_dev(s[0]), t=_dev(s[1]), u=_dev(s[2]))
+    f = plan.execute(_dev(c)).cpu().numpy()
+    ref = oracle.dirft3(_oracle_pts(x), c, 1, _oracle_pts(s))
+    assert oracle.rel_l2(f.ravel(), ref) < 2e-4
