@@ -379,7 +379,7 @@ void BatchPlan<T>::setpts(const int64_t *npts, const T *x, const T *y, const T *
   GBN_LAUNCH_CHECK();
   SubproblemArrays sa;
   nsub = build_subproblems(skeys.as<uint32_t>(), Mtot, nbins_total, (uint32_t)binvol,
-                           opts.gpu_maxsubprobsize, &sa, stream);
+                           S.maxsub, &sa, stream);
   sub_bin.release();
   sub_start.release();
   sub_count.release();

@@ -138,7 +138,7 @@ template <typename T> int info_dev(void *p, gbnufft_plan_info *info) {
     info->spread_smem = P.spread_smem;
     info->horner_err = P.horner_err;
     info->spread_variant = P.spread_variant_in_use();
-    info->maxsubprobsize = P.opts.gpu_maxsubprobsize;
+    info->maxsubprobsize = P.maxsub;
   });
 }
 

@@ -121,7 +121,7 @@ int spread_noalloc_f(int dim, const int64_t *n_grid, int64_t M, const float *x, 
     }
     SubproblemArrays sa;
     const int nsub = build_subproblems(skeys, (int)M, nb, cell_keys ? (uint32_t)binvol : 1u,
-                                       opts.gpu_maxsubprobsize, &sa, stream, &arena);
+                                       S.maxsub, &sa, stream, &arena);
     // the output starts at zero; nothing else in the scratch needs clearing
     // (bin counters are cleared inside build_subproblems)
     GBN_CUDA(cudaMemsetAsync(grid, 0, (size_t)cells * sizeof(float2), stream));

@@ -56,6 +56,7 @@ struct SpreadSetup {
   int method = 2;
   size_t smem = 0;
   SpreadConfig cfg{2, 256, 0};
+  int maxsub = 1024; // points per subproblem at most
 };
 template <typename T>
 SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts &opts,
@@ -89,6 +90,7 @@ public:
   int nbins[3] = {1, 1, 1};
   int nsub = 0;
   int cell_sorted = 0; // points sorted by (bin, cell in bin)
+  int maxsub = 1024;   // points per subproblem at most
   size_t spread_smem = 0;
   cudaStream_t stream = nullptr;
   StageTimes times;

@@ -596,7 +596,7 @@ __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
   T ar[NR], ai[NR];
 #pragma unroll
   for (int r = 0; r < NR; ++r) ar[r] = ai[r] = T(0);
-  int cur = -1;
+  int cur = -1; // run base (packed start cells)
   const T *kxl = kx + (lx + XS) * SK; // row lx - dx + XS is kxl - dx * SK
   auto flush = [&]() {
     const int rb = (cur >> 20) * Q + ((cur >> 10) & 1023) * px + (cur & 1023);
