@@ -253,6 +253,7 @@ def run_gpu(args):
     hbm_bytes = float(M) * (12 + 8 * nt) + nf_cells * 8.0 * nt
     hbm_ach = hbm_bytes / (spread_ms * 1e-3)
     hbm_peak = measured_peak("hbm_gbs")
+    traffic = SPREAD_DRAM_BYTES_PER_POINT * M * nt if kname == "spread_tile3v_kernel" else None
 
     tot_ms = torch.tensor([ms_batched, ms_plain, ms_e2e], dtype=torch.float64, device=dev)
     if world > 1:
@@ -284,12 +285,12 @@ def run_gpu(args):
         "gpu_launches": 2 * args.steps,
         "roofline": {"bound": "smem_atomic", "achieved": achieved / 1e9,
                      "peak": (peak / 1e9) if peak else None, "unit": "G atomic f32 adds/s",
-                     "frac": (achieved / peak) if peak else None, "traffic": SPREAD_TRAFFIC,
+                     "frac": (achieved / peak) if peak else None, "traffic": traffic,
                      "kernel": kname, "per_launch": atom_per_launch,
                      "peak_source": "measured by gbnufft_smem_atomic_rate on this GPU"},
         "roofline_hbm": {"bound": "hbm", "achieved": hbm_ach / 1e9, "peak": hbm_peak,
                          "unit": "GB/s", "frac": (hbm_ach / 1e9 / hbm_peak) if hbm_peak else None,
-                         "traffic": SPREAD_TRAFFIC, "kernel": kname,
+                         "traffic": traffic, "kernel": kname,
                          "algorithmic_bytes_per_launch": hbm_bytes,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "clocks": clk.summary(),
@@ -301,9 +302,11 @@ def run_gpu(args):
         dist.barrier()
 
 
-# DRAM bytes (read + write) of one spread launch from an ncu capture, scaled to
-# this workload; None until a capture of the default kernel is recorded
-SPREAD_TRAFFIC = None
+# DRAM bytes (read + write) per point per transform of the default 3D spread
+# kernel, from an ncu capture at the same point density (1.25e7 clustered
+# points on a 256^3 grid: 950.2 MB read + 132.4 MB written); scaled by points
+# and transforms to one launch of this workload
+SPREAD_DRAM_BYTES_PER_POINT = (950.213e6 + 132.354e6) / 12.5e6
 
 
 def measured_peak(key):
@@ -468,6 +471,22 @@ def run_config(args):
                                                     "p99": float(np.percentile(per, 99)),
                                                     "sample": len(per)},
                     "batched_ms_per_problem": ms / nprob})
+    elif args.config == "c3t2":
+        # 3D type 2 on the metric's points and sizes (the adjoint direction)
+        M = args.m
+        pts = clustered_points(M, 1234 + 3, rng_dev="cuda")
+        fk = torch.randn(*N_MODES, 2, generator=g, device="cuda").view(torch.complex64)[..., 0]
+        p = fg.Plan(2, N_MODES, eps=TOL, isign=-1, gpu_stream=stream.cuda_stream)
+        p.setpts(pts[0].contiguous(), pts[1].contiguous(), pts[2].contiguous())
+        cc = torch.empty(M, dtype=torch.complex64, device=dev)
+        ms = _timed(lambda: p.execute(fk, out=cc), stream, args.steps, args.warmup)
+        p.stage_times(True)
+        p.execute(fk, out=cc)
+        torch.cuda.synchronize()
+        st = p.stage_times(True)
+        out.update({"workload": "3D type 2 FP32, 256^3 modes, M=1e8 clustered, tol 1e-5",
+                    "value": M / (ms * 1e-3), "unit": "NU pts/s", "ms_per_step": ms,
+                    "stage_ms": {"interp": st[0], "fft": st[1], "amplify": st[2]}})
     elif args.config == "c5":
         # 3D type 3: M = K = 1e7, sources in box (1,2,4), targets in box (200,100,50)
         M = K = 10_000_000
@@ -532,7 +551,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4_000_000)
     ap.add_argument("--err-modes", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c4", "c5"],
+    ap.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c3t2", "c4", "c5"],
                     help="c3 (default) is the metric line; the others print their own line")
     ap.add_argument("--nmodes", type=int, default=0, help="modes per side (profiling cases)")
     ap.add_argument("--bins", default="", help="bin sizes x,y,z (default: the planner's)")

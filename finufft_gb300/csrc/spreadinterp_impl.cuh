@@ -8,6 +8,8 @@
 // support cell in tile coordinates is s = ceil(l - ns/2) + floor(ns/2) in
 // [0, bin] and its kernel weights are phi(ceil(l - ns/2) - l + j), j < ns.
 #pragma once
+#include <algorithm>
+#include <cstdlib>
 #include "device_util.cuh"
 #include "spreadinterp.h"
 #include "tile_layout.h"
@@ -220,7 +222,7 @@ __global__ void __launch_bounds__(256)
 // order of floating-point additions.
 template <typename T, int NS>
 __global__ void __launch_bounds__(256)
-    spread_tile3_kernel(PointLayout<T> L, KernelShape<T> K, const cplx<T> *__restrict__ c,
+    spread_tile3_kernel(PointLayout<T> L0, KernelShape<T> K, const cplx<T> *__restrict__ c,
                         const cplx<T> *__restrict__ pre, int conj_pre,
                         cplx<T> *__restrict__ fw, int64_t nf_total) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -230,7 +232,10 @@ __global__ void __launch_bounds__(256)
   constexpr int NROUND = (NPAIR + 3) / 4;
   const int sub = blockIdx.x;
   const int tr = blockIdx.y;
-  const int b = L.sub_bin[sub];
+  int b = L0.sub_bin[sub];
+  PointLayout<T> Lg;
+  const int64_t goff = resolve_problem<T>(L0, Lg, b);
+  const PointLayout<T> &L = Lg;
   const int p0 = L.sub_start[sub];
   const int np = L.sub_count[sub];
   const TileGeom<3> G = tile_of<T, 3, NS>(L, b);
@@ -305,7 +310,7 @@ __global__ void __launch_bounds__(256)
     __syncwarp();
   }
   __syncthreads();
-  cplx<T> *fwt = fw + (int64_t)tr * nf_total;
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total + goff;
   for (int q = threadIdx.x; q < G.cells; q += blockDim.x) {
     const int x = q % G.t[0];
     const int y = (q / G.t[0]) % G.t[1];
@@ -1163,6 +1168,7 @@ __global__ void __launch_bounds__(GLOBAL_SPREAD_THREADS)
 // Interpolation: one thread per point, gathering the NS^DIM support values of
 // the fine grid (read through L1/L2: the points of a subproblem share a tile).
 constexpr int INTERP_THREADS = 128;
+constexpr int INTERP_TILE_THREADS = 256;
 
 // Interpolation: one thread per point; the point's kernel weights and grid
 // indices are computed once and reused for every transform of the batch.
@@ -1266,6 +1272,116 @@ __global__ void __launch_bounds__(INTERP_THREADS)
   }
 }
 
+// Interpolation from a shared-memory tile (types 2 and 3, 2D and 3D): the
+// block stages its subproblem's (bin + ns)^d cells of the fine grid once per
+// transform with coalesced loads (periodic wrap applied while loading), for
+// up to tb transforms per round, then each thread evaluates its points'
+// weights once per round and reads the ns^d cells from shared memory.
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(INTERP_TILE_THREADS)
+    interp_tile_kernel(PointLayout<T> L0, KernelShape<T> K, const cplx<T> *__restrict__ fw,
+                       int64_t nf_total, const cplx<T> *__restrict__ post, int conj_post,
+                       cplx<T> *__restrict__ out, int ntr, int tb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int sub = blockIdx.x;
+  int b = L0.sub_bin[sub];
+  PointLayout<T> Lg;
+  const int64_t goff = resolve_problem<T>(L0, Lg, b);
+  const PointLayout<T> &L = Lg;
+  const int p0 = L.sub_start[sub];
+  const int np = L.sub_count[sub];
+  if (np <= 0) return;
+  const TileGeom<DIM> G = tile_of<T, DIM, NS>(L, b);
+  const int tx = G.t[0], ty = G.t[1];
+  const int cells = G.cells, txy = tx * ty;
+  cplx<T> *tile = reinterpret_cast<cplx<T> *>(smem_raw); // [tb][cells]
+  T *kzs = reinterpret_cast<T *>(tile + (size_t)tb * cells) + threadIdx.x * (NS + 1);
+  const int64_t plane = (int64_t)L.nf[0] * L.nf[1];
+  for (int t0 = 0; t0 < ntr; t0 += tb) {
+    const int nt = min(tb, ntr - t0);
+    __syncthreads(); // the previous round's readers are done
+    // rows of the tile (one per warp at a time, lanes along x): no per-cell division
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int rows = cells / tx;
+    for (int k = 0; k < nt; ++k) {
+      const cplx<T> *src = fw + (int64_t)(t0 + k) * nf_total + goff;
+      cplx<T> *dst = tile + (size_t)k * cells;
+      for (int r = threadIdx.x >> 5; r < rows; r += nw) {
+        int64_t rb = (int64_t)L.nf[0] * wrap_idx(G.org[1] + (DIM == 3 ? r % ty : r), L.nf[1]);
+        if constexpr (DIM == 3) rb += plane * wrap_idx(G.org[2] + r / ty, L.nf[2]);
+        for (int x = lane; x < tx; x += 32)
+          dst[r * tx + x] = src[rb + wrap_idx(G.org[0] + x, L.nf[0])];
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+      const int p = p0 + i;
+      const int j = L.perm[p];
+      T kx[NS], ky[NS];
+      const int sx = point_weights<T, NS>(L.loc[0][p], L.bin[0], K, kx);
+      const int sy = point_weights<T, NS>(L.loc[1][p], L.bin[1], K, ky);
+      int sz = 0;
+      if constexpr (DIM == 3) {
+        T kz[NS];
+        sz = point_weights<T, NS>(L.loc[2][p], L.bin[2], K, kz);
+#pragma unroll
+        for (int cc = 0; cc < NS; ++cc) kzs[cc] = kz[cc]; // read back with a dynamic index
+      }
+      cplx<T> pf;
+      pf.x = T(1);
+      pf.y = T(0);
+      if (post) {
+        pf = post[j];
+        if (conj_post) pf.y = -pf.y;
+      }
+      const int base = sz * txy + sy * tx + sx;
+#pragma unroll 1
+      for (int k = 0; k < nt; ++k) {
+        const cplx<T> *tl = tile + (size_t)k * cells + base;
+        T accr = T(0), acci = T(0);
+        if constexpr (DIM == 2) {
+#pragma unroll
+          for (int bb = 0; bb < NS; ++bb) {
+            T rr = T(0), ri = T(0);
+#pragma unroll
+            for (int a = 0; a < NS; ++a) {
+              const cplx<T> g = tl[bb * tx + a];
+              rr = fma(g.x, kx[a], rr);
+              ri = fma(g.y, kx[a], ri);
+            }
+            accr = fma(rr, ky[bb], accr);
+            acci = fma(ri, ky[bb], acci);
+          }
+        } else {
+#pragma unroll 1
+          for (int cc = 0; cc < NS; ++cc) {
+            const cplx<T> *tp = tl + cc * txy;
+            T pr = T(0), pi = T(0);
+#pragma unroll
+            for (int bb = 0; bb < NS; ++bb) {
+              T rr = T(0), ri = T(0);
+#pragma unroll
+              for (int a = 0; a < NS; ++a) {
+                const cplx<T> g = tp[bb * tx + a];
+                rr = fma(g.x, kx[a], rr);
+                ri = fma(g.y, kx[a], ri);
+              }
+              pr = fma(rr, ky[bb], pr);
+              pi = fma(ri, ky[bb], pi);
+            }
+            accr = fma(pr, kzs[cc], accr);
+            acci = fma(pi, kzs[cc], acci);
+          }
+        }
+        cplx<T> r;
+        r.x = accr * pf.x - acci * pf.y;
+        r.y = accr * pf.y + acci * pf.x;
+        out[(int64_t)(t0 + k) * L.M + j] = r;
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------- dispatch ----
 template <typename T, int DIM> struct Dispatch {
   template <int NS>
@@ -1322,6 +1438,31 @@ template <typename T, int DIM> struct Dispatch {
   static void interp(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *fw,
                      int64_t nf_total, const cplx<T> *post, int conj_post, cplx<T> *out,
                      int ntr, cudaStream_t s) {
+    if constexpr (DIM >= 2) {
+      // tile-staged interpolation when one transform's tile fits the per-block
+      // budget (three blocks per SM); GBNUFFT_INTERP_METHOD=0 keeps the gather
+      static const int imethod = [] {
+        const char *e = std::getenv("GBNUFFT_INTERP_METHOD");
+        return e ? std::atoi(e) : 1;
+      }();
+      size_t cells = 1;
+      for (int d = 0; d < DIM; ++d) cells *= (size_t)(L.bin[d] + NS);
+      const size_t tbytes = cells * sizeof(cplx<T>);
+      const size_t kzb = DIM == 3 ? (size_t)INTERP_TILE_THREADS * (NS + 1) * sizeof(T) : 0;
+      const size_t budget = 72 * 1024;
+      if (imethod != 0 && tbytes + kzb <= budget) {
+        int tb = (int)((budget - kzb) / tbytes);
+        tb = std::max(1, std::min(tb, std::min(ntr, 8)));
+        const size_t smem = (size_t)tb * tbytes + kzb;
+        auto kt = interp_tile_kernel<T, DIM, NS>;
+        GBN_CUDA(cudaFuncSetAttribute(kt, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        kt<<<(unsigned)L.nsub, INTERP_TILE_THREADS, smem, s>>>(L, K, fw, nf_total, post, conj_post,
+                                                         out, ntr, tb);
+        GBN_LAUNCH_CHECK();
+        return;
+      }
+    }
     interp_kernel<T, DIM, NS><<<(unsigned)L.nsub, INTERP_THREADS, 0, s>>>(L, K, fw, nf_total, post,
                                                                          conj_post, out, ntr);
     GBN_LAUNCH_CHECK();

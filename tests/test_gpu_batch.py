@@ -23,7 +23,7 @@ def _make_batch(rng, dim, nprob, nlo, nhi, mlo, mhi):
 
 
 @pytest.mark.parametrize("dim,ty,prec", [(2, 1, "f"), (2, 2, "f"), (3, 1, "f"), (1, 1, "f"),
-                                         (2, 1, "")])
+                                         (2, 1, ""), (3, 1, ""), (3, 2, "f")])
 def test_uneven_batch_matches_single_plans(oracle, engine, dim, ty, prec):
     import torch
 

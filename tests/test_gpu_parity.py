@@ -194,3 +194,43 @@ def test_spread_variants_type3(oracle, v):
     f = plan.execute(_dev(c)).cpu().numpy()
     ref = oracle.dirft3(_oracle_pts(x), c, 1, _oracle_pts(s))
     assert oracle.rel_l2(f.ravel(), ref) < 2e-4
+
+
+@pytest.mark.parametrize("dim,dtype", [(2, "complex64"), (3, "complex64"), (2, "complex128"),
+                                       (3, "complex128")])
+def test_type2_tile_rounds(oracle, dim, dtype):
+    """type 2 with 11 vectors (the tile-staged interpolation loads up to 8
+    transforms' tiles per round, so several rounds run), clustered points;
+    every vector equals its FP64 direct sum"""
+    import finufft_gb300 as fg
+
+    rdt = np.float32 if dtype == "complex64" else np.float64
+    tol = 1e-5 if dtype == "complex64" else 1e-11
+    rng = np.random.default_rng(90 + dim)
+    nm = (40, 36) if dim == 2 else (12, 14, 10)
+    M, ntr = 3000, 11
+    pts = _clustered(rng, dim, M, rdt)
+    fk = _cx(rng, (ntr,) + nm, dtype)
+    plan = fg.Plan(2, nm, n_trans=ntr, eps=tol, dtype=dtype, isign=-1)
+    plan.setpts(*[_dev(p) for p in pts])
+    c = plan.execute(_dev(fk)).cpu().numpy()
+    for k in (0, 5, 10):
+        ref = oracle.dirft2(_oracle_pts(pts), fk[k].ravel(), -1, nm[::-1])
+        assert oracle.rel_l2(c[k], ref) < 20 * tol, k
+
+
+def test_type3_adjoint_tile(oracle):
+    """the adjoint of type 3 interpolates with a post factor through the tile kernel"""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(95)
+    M, K = 3000, 500
+    x = _clustered(rng, 3, M, np.float64)
+    s = rng.uniform(-10, 10, (3, K))
+    f = _cx(rng, K, "complex128")
+    plan = fg.Plan(3, 3, eps=1e-10, dtype="complex128", isign=1)
+    plan.setpts(*[_dev(a) for a in x], s=_dev(s[0]), t=_dev(s[1]), u=_dev(s[2]))
+    c = plan.execute_adjoint(_dev(f)).cpu().numpy().ravel()
+    # adjoint of f_k = sum_j c_j e^{+i s_k x_j} is c_j = sum_k f_k e^{-i s_k x_j}
+    ref = oracle.dirft3(_oracle_pts(s), f, -1, _oracle_pts(x))
+    assert oracle.rel_l2(c, ref) < 1e-8
