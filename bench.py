@@ -113,6 +113,22 @@ def dist_info():
     return rank, world, local
 
 
+def reduce_over_ranks(ms, world, device):
+    """per-rank step times -> the slowest rank's (MAX over ranks; identity at N=1)"""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v) for v in ms], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def job_value(units_per_rank, world, ms):
+    """whole-job throughput: every rank processes units_per_rank per step (replicas)"""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 def time_steps(fn, stream, steps, warmup):
     import torch
 
@@ -255,14 +271,11 @@ def run_gpu(args):
     hbm_peak = measured_peak("hbm_gbs")
     traffic = SPREAD_DRAM_BYTES_PER_POINT * M * nt if kname == "spread_tile3v_kernel" else None
 
-    tot_ms = torch.tensor([ms_batched, ms_plain, ms_e2e], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(tot_ms, op=dist.ReduceOp.MAX)
-    ms_batched, ms_plain, ms_e2e = tot_ms.tolist()
+    ms_batched, ms_plain, ms_e2e = reduce_over_ranks([ms_batched, ms_plain, ms_e2e], world, dev)
     if rank != 0:
         dist.barrier() if world > 1 else None
         return
-    value = world * M * nt / (ms_batched * 1e-3)
+    value = job_value(M * nt, world, ms_batched)
     out = {
         "metric": METRIC, "value": value, "unit": "NU pts/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batched,
@@ -274,12 +287,12 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas",
                    "ns": ns, "nf": list(info.nf), "bins": list(info.bins),
                    "nsub": info.nsub},
-        "plain": {"value": world * M / (ms_plain * 1e-3), "ms_per_step": ms_plain,
+        "plain": {"value": job_value(M, world, ms_plain), "ms_per_step": ms_plain,
                   "stage_ms": {"spread": st[0], "fft": st[1], "deconv": st[2]}},
         "batched_stage_ms": {"spread": stb[0], "fft": stb[1], "deconv": stb[2]},
         "setpts_s": setpts_s,
         "rel_l2_err_sampled": err,
-        "e2e": {"value": world * M * nt / (ms_e2e * 1e-3), "unit": "NU pts/s",
+        "e2e": {"value": job_value(M * nt, world, ms_e2e), "unit": "NU pts/s",
                 "h2d_bytes_per_step": nt * M * 8, "d2h_bytes_per_step": nt * int(np.prod(N_MODES)) * 8,
                 "api": "finufftf_execute (host pointers, pinned)", "rel_diff_vs_device_api": e2e_err},
         "gpu_launches": 2 * args.steps,

@@ -85,7 +85,10 @@ def build(verbose=False, force=False, extra_nvcc=()):
                 logs.append(log)
     objs = [j[0] for j in jobs]
     if force or todo or not os.path.exists(LIB):
-        link = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcufft", "-lcudart"]
+        # SONAME libcufinufft.so: ctypes.util.find_library (the reference Python
+        # binding's system-path lookup) reports a library by its SONAME
+        link = [nvcc, *ARCH, "-shared", "-Xlinker", "-soname=libcufinufft.so", "-o", LIB, *objs,
+                "-lcufft", "-lcudart"]
         logs.append(_run(link))
     if verbose:
         for log in logs:

@@ -327,10 +327,14 @@ void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]
   AsyncBuf keys((size_t)std::max<int64_t>(Mp, 1) * 4, stream);
   AsyncBuf skeys((size_t)std::max<int64_t>(Mp, 1) * 4, stream);
   if (M > 0) {
-    launch_bin_keys<T>(dim, xyz, M, ax, nbins, cell_keys, keys.as<uint32_t>(), stream);
+    // one fold per point: the key pass also writes the bin-local coordinates,
+    // which are gathered into sorted order after the sort
+    AsyncBuf rec((size_t)Mp * 4 * sizeof(T), stream);
+    launch_bin_keys<T>(dim, xyz, M, ax, nbins, cell_keys, keys.as<uint32_t>(), stream,
+                       rec.as<T>());
     stable_sort_by_bin(keys.as<uint32_t>(), M, keybits, skeys.as<uint32_t>(), perm.p, stream);
     T *const lp[3] = {loc[0].p, dim > 1 ? loc[1].p : loc[0].p, dim > 2 ? loc[2].p : loc[0].p};
-    launch_sorted_local<T>(dim, xyz, perm.p, M, ax, lp, stream);
+    launch_gather_local<T>(dim, rec.as<T>(), perm.p, M, lp, stream);
   }
   SubproblemArrays sa;
   nsub = build_subproblems(skeys.as<uint32_t>(), M, nb, cell_keys ? (uint32_t)binvol : 1u,

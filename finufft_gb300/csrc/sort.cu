@@ -107,25 +107,65 @@ template <typename T, int DIM>
 __global__ void bin_key_kernel(const T *__restrict__ x, const T *__restrict__ y,
                                const T *__restrict__ z, int M, AxisMap a0, AxisMap a1,
                                AxisMap a2, int nb0, int nb1, int cell_keys,
-                               uint32_t *__restrict__ keys) {
+                               uint32_t *__restrict__ keys, T *__restrict__ rec) {
   const uint32_t binvol = (uint32_t)a0.bin * (DIM > 1 ? a1.bin : 1) * (DIM > 2 ? a2.bin : 1);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
     int c;
     double f;
+    T lc[4] = {T(0), T(0), T(0), T(0)};
     fold_cell((double)x[i], a0, c, f);
     uint32_t key = (uint32_t)(c / a0.bin);
     uint32_t loc = (uint32_t)(c - (c / a0.bin) * a0.bin);
+    lc[0] = (T)((double)(c - (c / a0.bin) * a0.bin) + f);
     if (DIM > 1) {
       fold_cell((double)y[i], a1, c, f);
       key += (uint32_t)nb0 * (uint32_t)(c / a1.bin);
       loc += (uint32_t)a0.bin * (uint32_t)(c - (c / a1.bin) * a1.bin);
+      lc[1] = (T)((double)(c - (c / a1.bin) * a1.bin) + f);
     }
     if (DIM > 2) {
       fold_cell((double)z[i], a2, c, f);
       key += (uint32_t)nb0 * (uint32_t)nb1 * (uint32_t)(c / a2.bin);
       loc += (uint32_t)a0.bin * (uint32_t)a1.bin * (uint32_t)(c - (c / a2.bin) * a2.bin);
+      lc[2] = (T)((double)(c - (c / a2.bin) * a2.bin) + f);
     }
     keys[i] = cell_keys ? key * binvol + loc : key;
+    if (rec) { // bin-local coordinates of point i as one aligned 4-element record
+      if constexpr (sizeof(T) == 4) {
+        reinterpret_cast<float4 *>(rec)[i] = make_float4(lc[0], lc[1], lc[2], 0.f);
+      } else {
+        double2 *r2 = reinterpret_cast<double2 *>(rec) + 2 * (size_t)i;
+        r2[0] = make_double2(lc[0], lc[1]);
+        r2[1] = make_double2(lc[2], 0.0);
+      }
+    }
+  }
+}
+
+// sorted bin-local coordinates gathered from the records the key pass wrote
+// (one 16- or 32-byte record per point instead of a refold of x, y, z)
+template <typename T, int DIM>
+__global__ void gather_local_kernel(const T *__restrict__ rec, const int *__restrict__ perm,
+                                    int M, T *__restrict__ l0, T *__restrict__ l1,
+                                    T *__restrict__ l2) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < M; p += gridDim.x * blockDim.x) {
+    const int i = perm[p];
+    T a, b = T(0), c = T(0);
+    if constexpr (sizeof(T) == 4) {
+      const float4 v = reinterpret_cast<const float4 *>(rec)[i];
+      a = v.x;
+      b = v.y;
+      c = v.z;
+    } else {
+      const double2 *r2 = reinterpret_cast<const double2 *>(rec) + 2 * (size_t)i;
+      const double2 u = r2[0];
+      a = u.x;
+      b = u.y;
+      if (DIM > 2) c = r2[1].x;
+    }
+    l0[p] = a;
+    if (DIM > 1) l1[p] = b;
+    if (DIM > 2) l2[p] = c;
   }
 }
 
@@ -161,20 +201,39 @@ inline unsigned grid_for(int64_t n, int threads) {
 
 template <typename T>
 void launch_bin_keys(int dim, const T *const xyz[3], int M, const AxisMap ax[3],
-                     const int nbin[3], int cell_keys, uint32_t *keys, cudaStream_t s) {
+                     const int nbin[3], int cell_keys, uint32_t *keys, cudaStream_t s,
+                     T *rec) {
   if (M <= 0) return;
   const unsigned g = grid_for(M, 256);
   if (dim == 1)
     bin_key_kernel<T, 1><<<g, 256, 0, s>>>(xyz[0], xyz[0], xyz[0], M, ax[0], ax[0], ax[0],
-                                           nbin[0], 1, cell_keys, keys);
+                                           nbin[0], 1, cell_keys, keys, rec);
   else if (dim == 2)
     bin_key_kernel<T, 2><<<g, 256, 0, s>>>(xyz[0], xyz[1], xyz[1], M, ax[0], ax[1], ax[1],
-                                           nbin[0], nbin[1], cell_keys, keys);
+                                           nbin[0], nbin[1], cell_keys, keys, rec);
   else
     bin_key_kernel<T, 3><<<g, 256, 0, s>>>(xyz[0], xyz[1], xyz[2], M, ax[0], ax[1], ax[2],
-                                           nbin[0], nbin[1], cell_keys, keys);
+                                           nbin[0], nbin[1], cell_keys, keys, rec);
   GBN_LAUNCH_CHECK();
 }
+
+template <typename T>
+void launch_gather_local(int dim, const T *rec, const int *perm, int M, T *const loc[3],
+                         cudaStream_t s) {
+  if (M <= 0) return;
+  const unsigned g = grid_for(M, 256);
+  if (dim == 1)
+    gather_local_kernel<T, 1><<<g, 256, 0, s>>>(rec, perm, M, loc[0], loc[0], loc[0]);
+  else if (dim == 2)
+    gather_local_kernel<T, 2><<<g, 256, 0, s>>>(rec, perm, M, loc[0], loc[1], loc[1]);
+  else
+    gather_local_kernel<T, 3><<<g, 256, 0, s>>>(rec, perm, M, loc[0], loc[1], loc[2]);
+  GBN_LAUNCH_CHECK();
+}
+template void launch_gather_local<float>(int, const float *, const int *, int,
+                                         float *const[3], cudaStream_t);
+template void launch_gather_local<double>(int, const double *, const int *, int,
+                                          double *const[3], cudaStream_t);
 
 template <typename T>
 void launch_sorted_local(int dim, const T *const xyz[3], const int *perm, int M,
@@ -194,9 +253,9 @@ void launch_sorted_local(int dim, const T *const xyz[3], const int *perm, int M,
 }
 
 template void launch_bin_keys<float>(int, const float *const[3], int, const AxisMap[3],
-                                     const int[3], int, uint32_t *, cudaStream_t);
+                                     const int[3], int, uint32_t *, cudaStream_t, float *);
 template void launch_bin_keys<double>(int, const double *const[3], int, const AxisMap[3],
-                                      const int[3], int, uint32_t *, cudaStream_t);
+                                      const int[3], int, uint32_t *, cudaStream_t, double *);
 template void launch_sorted_local<float>(int, const float *const[3], const int *, int,
                                          const AxisMap[3], float *const[3], cudaStream_t);
 template void launch_sorted_local<double>(int, const double *const[3], const int *, int,

@@ -50,8 +50,11 @@ void exclusive_scan_i32(const int *in, int *out, int64_t n, cudaStream_t s,
 // Sort key of every point: bin = bx + nb0*(by + nb1*bz) (x fastest); with
 // cell_keys, bin * binvol + the cell inside the bin (x fastest).
 template <typename T>
+// With rec non-null it also writes each point's bin-local coordinates, in
+// input order, as one record of 4 T (x, y, z, 0) at rec + 4 * i.
 void launch_bin_keys(int dim, const T *const xyz[3], int M, const AxisMap ax[3],
-                     const int nbin[3], int cell_keys, uint32_t *keys, cudaStream_t s);
+                     const int nbin[3], int cell_keys, uint32_t *keys, cudaStream_t s,
+                     T *rec = nullptr);
 
 // Stable LSD radix sort of (key, index) pairs by the low `keybits` bits of key.
 // On return perm_out[p] is the user index of the p-th point in bin order and
@@ -75,5 +78,9 @@ int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, uint32_t bi
 template <typename T>
 void launch_sorted_local(int dim, const T *const xyz[3], const int *perm, int M,
                          const AxisMap ax[3], T *const loc[3], cudaStream_t s);
+// The same from the records of launch_bin_keys (a gather, no refold).
+template <typename T>
+void launch_gather_local(int dim, const T *rec, const int *perm, int M, T *const loc[3],
+                         cudaStream_t s);
 
 } // namespace gbn

@@ -516,6 +516,14 @@ template <> struct Vec16<float> {
 template <> struct Vec16<double> {
   using type = double2;
 };
+// component u of a 16-byte vector and a vector from components (u is a
+// constant after unrolling, so these select registers without moves)
+__device__ __forceinline__ float vget(const float4 &v, int u) {
+  return u == 0 ? v.x : (u == 1 ? v.y : (u == 2 ? v.z : v.w));
+}
+__device__ __forceinline__ double vget(const double2 &v, int u) { return u == 0 ? v.x : v.y; }
+__device__ __forceinline__ float4 vmake(const float *e) { return make_float4(e[0], e[1], e[2], e[3]); }
+__device__ __forceinline__ double2 vmake(const double *e) { return make_double2(e[0], e[1]); }
 
 template <typename T, int NS>
 __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
@@ -625,31 +633,23 @@ __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
       for (int l4 = 0; l4 < 4; ++l4)
 #pragma unroll
         for (int v = 0; v < NRV; ++v) {
-          V w;
-          T *e = reinterpret_cast<T *>(&w);
+          T e[VW];
 #pragma unroll
           for (int u = 0; u < VW; ++u) {
             const int r = v * VW + u, pp = 4 * r + l4;
             e[u] = (r < NR && pp < NS * NS) ? kb[pp % NS] * kc[pp / NS] : T(0);
           }
-          pb[l4 * LPS + v] = w;
+          pb[l4 * LPS + v] = vmake(e);
         }
       const int spk = sx | (sy << 10) | (sz << 20);
-      V h;
-      T *he = reinterpret_cast<T *>(&h);
-      he[0] = pv.x;
-      he[1] = pv.y;
       if constexpr (VW == 4) {
-        he[2] = __int_as_float(spk);
-        he[3] = T(0);
-        pb[HDR] = h;
+        const float he[4] = {(float)pv.x, (float)pv.y, __int_as_float(spk), 0.f};
+        pb[HDR] = vmake(he);
       } else {
-        pb[HDR] = h;
-        V h2;
-        T *h2e = reinterpret_cast<T *>(&h2);
-        h2e[0] = __longlong_as_double((long long)spk);
-        h2e[1] = T(0);
-        pb[HDR + 1] = h2;
+        const double he[2] = {(double)pv.x, (double)pv.y};
+        const double h2[2] = {__longlong_as_double((long long)spk), 0.0};
+        pb[HDR] = vmake(he);
+        pb[HDR + 1] = vmake(h2);
       }
     }
     fetch(base + 32 + lane); // next batch, in flight while this one is summed
@@ -658,10 +658,9 @@ __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
     for (int q = 0; q < cnt; ++q) {
       const V *pq = pts + q * QS;
       const V h = pq[HDR];
-      const T *he = reinterpret_cast<const T *>(&h);
-      const T vr = he[0], vi = he[1];
+      const T vr = vget(h, 0), vi = vget(h, 1);
       int sp;
-      if constexpr (VW == 4) sp = __float_as_int(he[2]);
+      if constexpr (VW == 4) sp = __float_as_int(vget(h, 2));
       else sp = (int)__double_as_longlong(pq[HDR + 1].x);
       int dx = (sp & 1023) - (cur & 1023);
       if (((sp ^ cur) >> 10) != 0 || (unsigned)dx > (unsigned)XS) {
@@ -677,13 +676,13 @@ __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
 #pragma unroll
       for (int v = 0; v < NRV; ++v) {
         const V w = wl[v];
-        const T *e = reinterpret_cast<const T *>(&w);
 #pragma unroll
         for (int u = 0; u < VW; ++u) {
           const int r = v * VW + u;
           if (r < NR) {
-            ar[r] = fma(xr, e[u], ar[r]);
-            ai[r] = fma(xi, e[u], ai[r]);
+            const T wu = vget(w, u);
+            ar[r] = fma(xr, wu, ar[r]);
+            ai[r] = fma(xi, wu, ai[r]);
           }
         }
       }
