@@ -149,6 +149,8 @@ def _declare(lib):
     lib.gbnufft_default_opts.restype = None
     lib.gbnufft_smem_atomic_rate.argtypes = [c_int, POINTER(c_double)]
     lib.gbnufft_smem_atomic_rate.restype = c_int
+    lib.gbnufft_trim_scratch.argtypes = [c_int]
+    lib.gbnufft_trim_scratch.restype = c_int
     for pfx, real in (("finufft", c_double), ("finufftf", c_float)):
         f = getattr(lib, pfx + "_makeplan")
         f.argtypes = [c_int, c_int, i64p, c_int, c_int, real, POINTER(c_void_p),

@@ -12,6 +12,7 @@
 #include "finufft.h"
 #include "gbnufft_ext.h"
 #include "plan.h"
+#include "sort.h"
 
 using gbn::Plan;
 
@@ -289,6 +290,13 @@ GBN_EXT_DEFS(cufinufft, cufinufft_plan, double, cuDoubleComplex)
 GBN_EXT_DEFS(cufinufftf, cufinufftf_plan, float, cuFloatComplex)
 
 const char *gbnufft_version(void) { return "gb300-nufft 0.1 (sm_103a)"; }
+
+int gbnufft_trim_scratch(int device) {
+  return guarded([&] {
+    gbn::DeviceScope ds(device);
+    gbn::trim_scratch_pool();
+  });
+}
 
 int gbnufft_smem_atomic_rate(int device, double *rate) {
   return guarded([&] {

@@ -41,6 +41,69 @@ __host__ __device__ inline void fold_cell(double x, const AxisMap &a, int &cell,
   frac = r - fl;
 }
 
+// Single-precision fold for float coordinates on the identity map (types 1
+// and 2) with nf < 2^24: x/(2 pi) + 1/2 is formed as an unevaluated float sum
+// hi + lo (error-free product and sum: fma gives the exact rounding error of a
+// product, Knuth's two-sum that of a sum), so the fold keeps ~48 bits like the
+// FP64 fold while running on the FP32 pipe. Every operation is rounded to
+// nearest with no contraction, so a host replica (fmaf) reproduces it bit for
+// bit. NaN/Inf coordinates land on cell 0.
+__host__ __device__ inline void fold_cell_f32(float x, int nf, int &cell, float &frac) {
+  constexpr float C_HI = (float)INV_2PI;
+  constexpr float C_LO = (float)(INV_2PI - (double)(float)INV_2PI);
+  const float nff = (float)nf;
+  if (!(x - x == 0.f)) { // NaN or Inf
+    cell = 0;
+    frac = 0.f;
+    return;
+  }
+#ifdef __CUDA_ARCH__
+#define GBN_MUL(a, b) __fmul_rn(a, b)
+#define GBN_ADD(a, b) __fadd_rn(a, b)
+#define GBN_SUB(a, b) __fsub_rn(a, b)
+#define GBN_FMA(a, b, c) __fmaf_rn(a, b, c)
+#else
+#define GBN_MUL(a, b) ((a) * (b))
+#define GBN_ADD(a, b) ((a) + (b))
+#define GBN_SUB(a, b) ((a) - (b))
+#define GBN_FMA(a, b, c) fmaf(a, b, c)
+#endif
+  // x/2pi + 1/2 = s + lo exactly enough: error-free product, then two-sum
+  const float ph = GBN_MUL(x, C_HI);
+  const float pl = GBN_FMA(x, C_LO, GBN_FMA(x, C_HI, -ph));
+  const float s = GBN_ADD(ph, 0.5f);
+  const float bb = GBN_SUB(s, ph);
+  const float lo = GBN_ADD(GBN_ADD(GBN_SUB(ph, GBN_SUB(s, bb)), GBN_SUB(0.5f, bb)), pl);
+  // fraction of s as an exact two-sum (s - floor(s) rounds to 1 for a tiny
+  // negative s): fh + fl, then scaled by nf: gh + gl
+  const float fls = -floorf(s);
+  const float fh = GBN_ADD(s, fls);
+  const float fb = GBN_SUB(fh, s);
+  const float fl = GBN_ADD(GBN_SUB(s, GBN_SUB(fh, fb)), GBN_SUB(fls, fb));
+  const float gh = GBN_MUL(fh, nff);
+  const float gl = GBN_FMA(GBN_ADD(fl, lo), nff, GBN_FMA(fh, nff, -gh));
+  float c = floorf(gh);
+  float fr = GBN_ADD(GBN_SUB(gh, c), gl);
+  // |gl| < 2, so fr is in (-2, 3): move its integer part into the cell; a tiny
+  // negative fraction plus one rounds to 1, which goes to the next cell
+  const float k = floorf(fr);
+  c = GBN_ADD(c, k);
+  fr = GBN_SUB(fr, k);
+  if (fr >= 1.f) {
+    c = GBN_ADD(c, 1.f);
+    fr = 0.f;
+  }
+#undef GBN_MUL
+#undef GBN_ADD
+#undef GBN_SUB
+#undef GBN_FMA
+  int ci = (int)c;
+  if (ci < 0) ci += nf;
+  else if (ci >= nf) ci -= nf;
+  cell = ci;
+  frac = fr;
+}
+
 #ifdef __CUDACC__
 template <typename T> __device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
   cplx<T> r;

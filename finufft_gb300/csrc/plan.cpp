@@ -336,16 +336,18 @@ void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]
     T *const lp[3] = {loc[0].p, dim > 1 ? loc[1].p : loc[0].p, dim > 2 ? loc[2].p : loc[0].p};
     launch_gather_local<T>(dim, rec.as<T>(), perm.p, M, lp, stream);
   }
+  // the subproblem arrays are reused while they hold enough entries
   SubproblemArrays sa;
+  sa.bin = sub_bin_.p;
+  sa.start = sub_start_.p;
+  sa.count = sub_count_.p;
+  sa.cap = sub_bin_.n;
   nsub = build_subproblems(skeys.as<uint32_t>(), M, nb, cell_keys ? (uint32_t)binvol : 1u,
                            maxsub, &sa, stream);
-  sub_bin_.release();
-  sub_start_.release();
-  sub_count_.release();
   sub_bin_.p = sa.bin;
   sub_start_.p = sa.start;
   sub_count_.p = sa.count;
-  sub_bin_.n = sub_start_.n = sub_count_.n = (size_t)std::max(nsub, 1);
+  sub_bin_.n = sub_start_.n = sub_count_.n = sa.cap;
 }
 
 template <typename T>

@@ -9,6 +9,9 @@
 // for the CPU library's bin ordering: x fastest, then y, then z).
 #include "sort.h"
 
+#include <map>
+#include <mutex>
+
 namespace gbn {
 
 // ---------------------------------------------------------------- scan ----
@@ -109,6 +112,45 @@ __global__ void bin_key_kernel(const T *__restrict__ x, const T *__restrict__ y,
                                AxisMap a2, int nb0, int nb1, int cell_keys,
                                uint32_t *__restrict__ keys, T *__restrict__ rec) {
   const uint32_t binvol = (uint32_t)a0.bin * (DIM > 1 ? a1.bin : 1) * (DIM > 2 ? a2.bin : 1);
+  // float coordinates on the identity map: single-precision fold and a
+  // reciprocal division (exact below 2^20 cells after one correction step)
+  const AxisMap am[3] = {a0, a1, a2};
+  bool f32 = sizeof(T) == 4;
+  for (int d = 0; d < DIM; ++d)
+    f32 = f32 && am[d].shift == 0.0 && am[d].scale == 1.0 && am[d].nf < (1 << 20);
+  if constexpr (sizeof(T) == 4) if (f32) {
+    const T *const xs[3] = {x, y, z};
+    float inv[3];
+    for (int d = 0; d < DIM; ++d) inv[d] = 1.0f / (float)am[d].bin;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+      T lc[4] = {T(0), T(0), T(0), T(0)};
+      uint32_t key = 0, loc = 0, ks = 1, ls = 1;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        int c;
+        float f;
+        fold_cell_f32((float)xs[d][i], am[d].nf, c, f);
+        const int b = am[d].bin;
+        int q = __float2int_rz(__fmul_rn((float)c, inv[d]));
+        int r = c - q * b;
+        if (r < 0) {
+          --q;
+          r += b;
+        } else if (r >= b) {
+          ++q;
+          r -= b;
+        }
+        key += ks * (uint32_t)q;
+        loc += ls * (uint32_t)r;
+        ks *= (uint32_t)(d == 0 ? nb0 : nb1);
+        ls *= (uint32_t)b;
+        lc[d] = (T)__fadd_rn((float)r, f);
+      }
+      keys[i] = cell_keys ? key * binvol + loc : key;
+      if (rec) reinterpret_cast<float4 *>(rec)[i] = make_float4(lc[0], lc[1], lc[2], 0.f);
+    }
+    return;
+  }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
     int c;
     double f;
@@ -292,6 +334,9 @@ __global__ void radix_scatter_kernel(const uint32_t *__restrict__ kin,
                                      int *__restrict__ vout, int M, int shift, int ntiles,
                                      const int *__restrict__ offs) {
   __shared__ int wcnt[RS_WARPS][256];
+  __shared__ int dstart[257];               // first tile position of each digit
+  __shared__ uint32_t tk[RS_TILE];          // the tile's keys in (digit, input) order
+  __shared__ int tv[RS_TILE];               // and their values
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < RS_WARPS * 256; i += blockDim.x) (&wcnt[0][0])[i] = 0;
   __syncthreads();
@@ -315,25 +360,55 @@ __global__ void radix_scatter_kernel(const uint32_t *__restrict__ kin,
     rank[j] = r;
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < 256; d += blockDim.x) {
-    int run = 0;
+  // per digit: warp offsets inside the digit, and the digit's tile total
+  int total = 0;
+  if (threadIdx.x < 256) {
+    const int d = threadIdx.x;
 #pragma unroll
     for (int ww = 0; ww < RS_WARPS; ++ww) {
       const int t = wcnt[ww][d];
-      wcnt[ww][d] = run;
-      run += t;
+      wcnt[ww][d] = total;
+      total += t;
     }
   }
+  // exclusive scan of the 256 digit totals (thread d holds digit d; 256 threads)
+  {
+    int v = total;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+    __shared__ int wsum[RS_WARPS];
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    int add = 0;
+    for (int ww = 0; ww < w; ++ww) add += wsum[ww];
+    if (threadIdx.x < 256) dstart[threadIdx.x] = v - total + add;
+  }
   __syncthreads();
+  // reorder the tile by digit in shared memory (stable: ranks follow input order)
 #pragma unroll
   for (int j = 0; j < RS_ITEMS; ++j) {
     const int64_t i = base + j * 32 + lane;
     if (i < M) {
       const int d = (int)((key[j] >> shift) & 255u);
-      const int pos = offs[(int64_t)d * ntiles + blockIdx.x] + wcnt[w][d] + rank[j];
-      kout[pos] = key[j];
-      vout[pos] = vin ? vin[i] : (int)i;
+      const int t = dstart[d] + wcnt[w][d] + rank[j];
+      tk[t] = key[j];
+      tv[t] = vin ? vin[i] : (int)i;
     }
+  }
+  __syncthreads();
+  // write out in tile order: consecutive threads store consecutive positions of
+  // each digit's run
+  const int64_t tile0 = (int64_t)blockIdx.x * RS_TILE;
+  const int n = (int)min((int64_t)RS_TILE, (int64_t)M - tile0);
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const uint32_t k = tk[t];
+    const int d = (int)((k >> shift) & 255u);
+    const int pos = offs[(int64_t)d * ntiles + blockIdx.x] + (t - dstart[d]);
+    kout[pos] = k;
+    vout[pos] = tv[t];
   }
 }
 
@@ -410,6 +485,30 @@ __global__ void fill_subproblems_kernel(const int *__restrict__ bstart, const in
 }
 } // namespace
 
+cudaMemPool_t scratch_pool() {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  int dev = 0;
+  GBN_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = pools.find(dev);
+  if (it != pools.end()) return it->second;
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool;
+  GBN_CUDA(cudaMemPoolCreate(&pool, &props));
+  uint64_t keep = UINT64_MAX;
+  GBN_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  pools[dev] = pool;
+  return pool;
+}
+
+void trim_scratch_pool() {
+  cudaMemPoolTrimTo(scratch_pool(), 0);
+}
+
 int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, uint32_t binvol,
                       int maxsub, SubproblemArrays *out, cudaStream_t s, Arena *arena) {
   AsyncBuf bstart((size_t)nbins * 4, s, arena), bcnt((size_t)nbins * 4, s, arena),
@@ -435,14 +534,16 @@ int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, uint32_t bi
     out->bin = (int *)arena->take(nalloc);
     out->start = (int *)arena->take(nalloc);
     out->count = (int *)arena->take(nalloc);
-  } else {
+  } else if (!out->bin || out->cap * 4 < nalloc) {
     if (out->bin) cudaFree(out->bin);
     if (out->start) cudaFree(out->start);
     if (out->count) cudaFree(out->count);
     out->bin = out->start = out->count = nullptr;
+    out->cap = 0;
     GBN_CUDA(cudaMalloc(&out->bin, nalloc));
     GBN_CUDA(cudaMalloc(&out->start, nalloc));
     GBN_CUDA(cudaMalloc(&out->count, nalloc));
+    out->cap = nalloc / 4;
   }
   fill_subproblems_kernel<<<grid_for(nbins, 256), 256, 0, s>>>(
       bstart.as<int>(), bcnt.as<int>(), nsub.as<int>(), substart.as<int>(), nbins, maxsub,

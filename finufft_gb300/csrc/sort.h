@@ -21,6 +21,14 @@ struct Arena {
 
 // Device scratch: from an Arena when one is given, else stream-ordered
 // cudaMallocAsync / cudaFreeAsync.
+// Stream-ordered pool of the current device for setpts scratch (keys,
+// records, sort buffers). It keeps freed memory for the next setpts instead of
+// returning it to the driver at every synchronisation (the default pool's
+// behaviour), which would re-map gigabytes per call; gbnufft_trim_scratch
+// releases it.
+cudaMemPool_t scratch_pool();
+void trim_scratch_pool(); // release the current device's cached scratch
+
 struct AsyncBuf {
   void *p = nullptr;
   cudaStream_t s = nullptr;
@@ -31,7 +39,7 @@ struct AsyncBuf {
     if (arena) {
       p = arena->take(bytes);
     } else {
-      GBN_CUDA(cudaMallocAsync(&p, bytes, st));
+      GBN_CUDA(cudaMallocFromPoolAsync(&p, bytes, scratch_pool(), st));
       owned = true;
     }
   }
@@ -66,10 +74,11 @@ void stable_sort_by_bin(uint32_t *keys_in, int M, int keybits, uint32_t *keys_ou
 // Returns the number of subproblems (one device->host copy, stream sync).
 struct SubproblemArrays {
   int *bin = nullptr, *start = nullptr, *count = nullptr;
+  size_t cap = 0; // entries the three arrays hold
 };
 // binvol: keys per bin (1 for plain bin keys). With an arena the three output
-// arrays are carved from it (nothing to free); otherwise they are cudaMalloc'd
-// and the previous contents of *out are cudaFree'd.
+// arrays are carved from it (nothing to free); otherwise the arrays in *out
+// are kept when they hold enough entries, else cudaFree'd and cudaMalloc'd.
 int build_subproblems(const uint32_t *sorted_keys, int M, int nbins, uint32_t binvol,
                       int maxsub, SubproblemArrays *out, cudaStream_t s,
                       Arena *arena = nullptr);

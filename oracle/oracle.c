@@ -170,6 +170,77 @@ void or_fold_cell(double x, double shift, double scale, int nf, int *cell, doubl
   *frac = r - fl;
 }
 
+/* The engine's single-precision fold for float coordinates on the identity
+ * map (shift 0, scale 1, nf < 2^20): x/2pi + 1/2 as an unevaluated float sum
+ * (error-free product by fmaf, two-sum), its fraction times nf as another,
+ * then the integer part of the fraction moved into the cell; NaN/Inf -> cell 0. Every
+ * step is a float operation rounded to nearest (-ffp-contract=off). */
+void or_fold_cell_f32(float x, int nf, int *cell, float *frac) {
+  const float c_hi = (float)OR_INV_2PI;
+  const float c_lo = (float)(OR_INV_2PI - (double)c_hi);
+  const float nff = (float)nf;
+  if (!(x - x == 0.f)) { /* NaN or Inf */
+    *cell = 0;
+    *frac = 0.f;
+    return;
+  }
+  const float ph = x * c_hi;
+  const float pl = fmaf(x, c_lo, fmaf(x, c_hi, -ph));
+  const float s = ph + 0.5f;
+  const float bb = s - ph;
+  const float lo = ((ph - (s - bb)) + (0.5f - bb)) + pl;
+  /* fraction of s as an exact two-sum, then times nf */
+  const float fls = -floorf(s);
+  const float fh = s + fls;
+  const float fb = fh - s;
+  const float fl = (s - (fh - fb)) + (fls - fb);
+  const float gh = fh * nff;
+  const float gl = fmaf(fl + lo, nff, fmaf(fh, nff, -gh));
+  float c = floorf(gh);
+  float fr = (gh - c) + gl;
+  const float k = floorf(fr); /* fr in (-2, 3) */
+  c = c + k;
+  fr = fr - k;
+  if (fr >= 1.f) { /* a tiny negative fraction plus one rounded to 1 */
+    c = c + 1.f;
+    fr = 0.f;
+  }
+  int ci = (int)c;
+  if (ci < 0) ci += nf;
+  else if (ci >= nf) ci -= nf;
+  *cell = ci;
+  *frac = fr;
+}
+
+/* both folds over an array of float coordinates (accuracy checks):
+ * grid position cell + frac of each */
+void or_fold_many(int64_t n, const float *x, int nf, int f32, int *cell, double *frac) {
+  for (int64_t i = 0; i < n; ++i) {
+    if (f32) {
+      float f;
+      or_fold_cell_f32(x[i], nf, &cell[i], &f);
+      frac[i] = f;
+    } else {
+      or_fold_cell((double)x[i], 0.0, 1.0, nf, &cell[i], &frac[i]);
+    }
+  }
+}
+
+/* one axis of a point: cell, and the bin-local coordinate in double (FP64
+ * fold) or as the float the single-precision path stores */
+static void or_axis(double x, double shift, double scale, int nf, int bin, int f32, int *cell,
+                    double *local) {
+  if (f32) {
+    float f;
+    or_fold_cell_f32((float)x, nf, cell, &f);
+    *local = (double)((float)(*cell % bin) + f);
+  } else {
+    double f;
+    or_fold_cell(x, shift, scale, nf, cell, &f);
+    *local = (double)(*cell - (*cell / bin) * bin) + f;
+  }
+}
+
 /* Stable counting sort of the points, as the CPU library's bin sort
  * (include/finufft/spread.hpp:459-584: bins x fastest, input order kept inside
  * a key) with the engine's fold and integer bins. The key is the bin, times the
@@ -177,10 +248,12 @@ void or_fold_cell(double x, double shift, double scale, int nf, int *cell, doubl
  * bins * bin volume fits 32 bits -- the engine's device key.
  * coords: dim arrays of doubles (float inputs converted exactly). Outputs
  * perm[M] and loc[dim*M] (bin-local coordinates, rounded to float when
- * loc_is_float). Returns 0. */
+ * loc_is_float; with float_inputs (coordinates given as floats) and the
+ * identity map they take the single-precision fold, as the engine's device
+ * sort does for float plans). Returns 0. */
 int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *shift,
                 const double *scale, const int *nf, const int *bin, int32_t *perm,
-                void *loc, int loc_is_float) {
+                void *loc, int loc_is_float, int float_inputs) {
   int nb[3] = {1, 1, 1};
   int bn[3] = {1, 1, 1};
   for (int d = 0; d < dim; ++d) {
@@ -191,14 +264,17 @@ int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *s
   const uint64_t binvol = (uint64_t)bn[0] * bn[1] * bn[2];
   const int cell_keys = nbins * binvol <= 0xffffffffull;
   const uint64_t nkeys = cell_keys ? nbins * binvol : nbins;
+  int f32 = loc_is_float && float_inputs;
+  for (int d = 0; d < dim; ++d)
+    f32 = f32 && shift[d] == 0.0 && scale[d] == 1.0 && nf[d] < (1 << 20);
   int64_t *cnt = (int64_t *)calloc((size_t)nkeys + 1, sizeof(int64_t));
   uint32_t *key = (uint32_t *)malloc((size_t)(M > 0 ? M : 1) * sizeof(uint32_t));
   for (int64_t i = 0; i < M; ++i) {
     uint32_t k = 0, stride = 1, lc = 0, lstride = 1;
     for (int d = 0; d < dim; ++d) {
       int c;
-      double f;
-      or_fold_cell(coords[d][i], shift[d], scale[d], nf[d], &c, &f);
+      double l;
+      or_axis(coords[d][i], shift[d], scale[d], nf[d], bin[d], f32, &c, &l);
       k += stride * (uint32_t)(c / bin[d]);
       lc += lstride * (uint32_t)(c - (c / bin[d]) * bin[d]);
       stride *= (uint32_t)nb[d];
@@ -213,9 +289,8 @@ int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *s
     int64_t i = perm[p];
     for (int d = 0; d < dim; ++d) {
       int c;
-      double f;
-      or_fold_cell(coords[d][i], shift[d], scale[d], nf[d], &c, &f);
-      double l = (double)(c - (c / bin[d]) * bin[d]) + f;
+      double l;
+      or_axis(coords[d][i], shift[d], scale[d], nf[d], bin[d], f32, &c, &l);
       if (loc_is_float) ((float *)loc)[(size_t)d * M + p] = (float)l;
       else ((double *)loc)[(size_t)d * M + p] = l;
     }

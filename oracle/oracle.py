@@ -49,7 +49,8 @@ def lib():
         L.or_fine_grid.argtypes = [I64, d, i]
         L.or_fine_grid.restype = I64
         L.or_type3_grid.argtypes = [d, d, d, i, P]
-        L.or_bin_sort.argtypes = [i, I64, P, P, P, P, P, P, P, i]
+        L.or_bin_sort.argtypes = [i, I64, P, P, P, P, P, P, P, i, i]
+        L.or_fold_many.argtypes = [I64, P, i, i, P, P]
         L.or_dirft1.argtypes = [i, I64, P, P, i, P, I64, P, P]
         L.or_dirft2.argtypes = [i, I64, P, i, P, P, I64, P, P]
         L.or_dirft3.argtypes = [i, I64, P, P, i, P, I64, P, P]
@@ -240,9 +241,20 @@ def rel_l2(a, b):
 
 
 # ------------------------------------------------------------ bin sort ----
+def fold_positions(x, nf, f32):
+    """grid positions cell + frac of float coordinates x under the engine's
+    single-precision fold (f32) or its FP64 fold: (cell int32, frac float64)"""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    cell = np.zeros(max(len(x), 1), np.int32)
+    frac = np.zeros(max(len(x), 1), np.float64)
+    lib().or_fold_many(len(x), _ptr(x), int(nf), int(f32), _ptr(cell), _ptr(frac))
+    return cell[:len(x)], frac[:len(x)]
+
+
 def bin_sort(xs, nf, bins, shift=None, scale=None, loc_dtype=np.float32):
     """Host replica of the device bin sort: (perm, loc[dim, M])."""
     dim = len(xs)
+    float_inputs = all(np.asarray(x).dtype == np.float32 for x in xs)
     xs = _coords(xs)
     M = len(xs[0])
     shift = np.zeros(3) if shift is None else np.asarray(list(shift) + [0] * (3 - dim), np.float64)
@@ -252,7 +264,7 @@ def bin_sort(xs, nf, bins, shift=None, scale=None, loc_dtype=np.float32):
     perm = np.zeros(max(M, 1), dtype=np.int32)
     loc = np.zeros((dim, max(M, 1)), dtype=loc_dtype)
     lib().or_bin_sort(dim, M, _ptrs(xs), _ptr(shift), _ptr(scale), _ptr(nfa), _ptr(ba),
-                      _ptr(perm), _ptr(loc), int(loc_dtype == np.float32))
+                      _ptr(perm), _ptr(loc), int(loc_dtype == np.float32), int(float_inputs))
     return perm[:M], loc[:, :M]
 
 

@@ -132,8 +132,10 @@ def test_sort_bit_exact(oracle, dtype, dim):
     loc = np.zeros(dim * M, dtype=rdt)
     fn = getattr(plan._lib, plan._pfx + "_get_sort")
     assert fn(plan._plan, perm.ctypes.data, loc.ctypes.data) == 0
-    hperm, hloc = oracle.bin_sort(_oracle_pts(pts), list(info.nf)[:dim], list(info.bins)[:dim],
-                                  loc_dtype=rdt)
+    # the coordinates as the engine received them (float32 for complex64 plans,
+    # which take the single-precision fold), fastest axis first
+    hperm, hloc = oracle.bin_sort([np.ascontiguousarray(p) for p in pts[::-1]],
+                                  list(info.nf)[:dim], list(info.bins)[:dim], loc_dtype=rdt)
     np.testing.assert_array_equal(perm, hperm)
     np.testing.assert_array_equal(loc.reshape(dim, M), hloc)
 
@@ -234,3 +236,33 @@ def test_type3_adjoint_tile(oracle):
     # adjoint of f_k = sum_j c_j e^{+i s_k x_j} is c_j = sum_k f_k e^{-i s_k x_j}
     ref = oracle.dirft3(_oracle_pts(s), f, -1, _oracle_pts(x))
     assert oracle.rel_l2(c, ref) < 1e-8
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_type1_cell_edge_points(oracle, dim):
+    """Float coordinates on, and one float step either side of, fine-grid cell
+    edges (where the single-precision fold's rounding is decided), including a
+    coordinate 1e-8 cells below an edge: every point must land within rounding
+    of its true position (one point a cell off would put the error near 1e-2)."""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(60 + dim)
+    nm = {1: (100,), 2: (40, 32), 3: (16, 20, 12)}[dim]
+    plan = fg.Plan(1, nm, eps=1e-5, dtype="complex64", isign=1)
+    nf = list(plan.info().nf)[:dim][::-1]  # row-major axis order (slowest first)
+    M = 3000
+    pts = []
+    for d in range(dim):
+        j = rng.integers(0, nf[d] + 1, M)
+        e = (2 * np.pi * (j / nf[d] - 0.5)).astype(np.float32)
+        step = rng.integers(-1, 2, M)
+        e = np.where(step > 0, np.nextafter(e, np.float32(9)),
+                     np.where(step < 0, np.nextafter(e, np.float32(-9)), e)).astype(np.float32)
+        pts.append(e)
+    pts = np.array(pts)
+    pts[0, :5] = np.uint32([3158904795]).view(np.float32)[0]
+    c = _cx(rng, M, "complex64")
+    plan.setpts(*[_dev(p) for p in pts])
+    f = plan.execute(_dev(c)).cpu().numpy()
+    ref = oracle.dirft1(_oracle_pts(pts), c, 1, nm[::-1]).reshape(nm)
+    assert oracle.rel_l2(f, ref) < 1e-4

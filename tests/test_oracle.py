@@ -157,3 +157,31 @@ def test_bin_sort_is_stable_and_bin_ordered(oracle):
     assert np.mean(np.diff(ks) >= 0) > 0.999
     same = np.diff(ks) == 0
     assert np.all(np.diff(perm)[same] > 0)
+
+
+def test_single_precision_fold_matches_fp64_fold(oracle):
+    """The engine's float fold (error-free float arithmetic) places float
+    coordinates where the FP64 fold does: same cell except within 1e-6 of a
+    cell edge, grid positions equal to ~1e-12 of the grid, including the
+    period seam, exact multiples of pi and large |x|."""
+    rng = np.random.default_rng(5)
+    base = np.concatenate([rng.uniform(-np.pi, np.pi, 200000), rng.uniform(-50, 50, 50000),
+                           np.float32([0.0, np.pi, -np.pi, 3 * np.pi, -np.float32(np.pi),
+                                       np.nextafter(np.float32(np.pi), np.float32(0))]),
+                           # a coordinate 1e-8 cells below a cell edge on a 512 grid
+                           np.uint32([3158904795]).view(np.float32)]).astype(np.float32)
+    for nf in (16, 512, 2048, 100000, (1 << 20) - 2):
+        # coordinates on and next to every cell edge (all edges for small grids)
+        j = np.arange(0, nf + 1, max(1, nf // 4096))
+        e = (2 * np.pi * (j / nf - 0.5)).astype(np.float32)
+        x = np.concatenate([base, e, np.nextafter(e, np.float32(9)), np.nextafter(e, np.float32(-9))])
+        c1, f1 = oracle.fold_positions(x, nf, True)
+        c0, f0 = oracle.fold_positions(x, nf, False)
+        assert ((c1 >= 0) & (c1 < nf)).all() and ((f1 >= 0) & (f1 <= 1)).all()
+        # positions on the circle of length nf
+        d = (c1 + f1) - (c0 + f0)
+        d = np.where(d > nf / 2, d - nf, np.where(d < -nf / 2, d + nf, d))
+        assert np.abs(d).max() < 1e-12 * nf + 1e-7, nf  # float frac rounding: < 6e-8
+        same = c1 == c0
+        edge = np.minimum(f0, 1 - f0) < 1e-6
+        assert (same | edge).all(), nf
