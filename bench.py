@@ -199,9 +199,15 @@ def run_gpu(args):
     torch.cuda.empty_cache()
 
     # planned + batched form: nt vectors sharing the points, graph replay
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     bplan = fg.Plan(1, N_MODES, n_trans=nt, eps=TOL, dtype="complex64",
                     gpu_stream=stream.cuda_stream, gpu_maxbatchsize=nt, **plan_kw)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
     bplan.setpts(x, y, z)
+    torch.cuda.synchronize()
+    makeplan_s, bsetpts_s = t1 - t0, time.perf_counter() - t1
     fkb = torch.empty((nt,) + N_MODES, dtype=torch.complex64, device=dev)
     bplan.execute(c, out=fkb)
     torch.cuda.synchronize()
@@ -291,6 +297,10 @@ def run_gpu(args):
                   "stage_ms": {"spread": st[0], "fft": st[1], "deconv": st[2]}},
         "batched_stage_ms": {"spread": stb[0], "fft": stb[1], "deconv": stb[2]},
         "setpts_s": setpts_s,
+        # the reference perftest's amortized figure (perftest/cuda/cuperftest.cu:401):
+        # points over makeplan + setpts + one execute, batched plan
+        "amortized": {"value": job_value(M * nt, world, (makeplan_s + bsetpts_s) * 1e3 + ms_batched),
+                      "unit": "NU pts/s", "makeplan_s": makeplan_s, "setpts_s": bsetpts_s},
         "rel_l2_err_sampled": err,
         "e2e": {"value": job_value(M * nt, world, ms_e2e), "unit": "NU pts/s",
                 "h2d_bytes_per_step": nt * M * 8, "d2h_bytes_per_step": nt * int(np.prod(N_MODES)) * 8,

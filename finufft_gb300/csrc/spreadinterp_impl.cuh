@@ -509,6 +509,30 @@ __global__ void __launch_bounds__(t3m_threads<T>(), 2)
 // its share as 16-byte vectors, the next batch's points are fetched while the
 // current batch is summed, and with (bin, cell)-sorted points only the z planes
 // the subproblem can touch are cleared and written back.
+// 32-bit shared-memory loads for the interpolation tile: a row's address is
+// formed once and its cells are read at constant offsets. volatile keeps them
+// ordered against the block barriers around each tile reload (the tile does
+// not change between barriers, so no memory clobber is needed).
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void lds_cplx(uint32_t a, float &x, float &y) {
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(x), "=f"(y) : "r"(a));
+}
+__device__ __forceinline__ void lds_cplx(uint32_t a, double &x, double &y) {
+  asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(x), "=d"(y) : "r"(a));
+}
+__device__ __forceinline__ float lds_real(uint32_t a, float) {
+  float x;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(x) : "r"(a));
+  return x;
+}
+__device__ __forceinline__ double lds_real(uint32_t a, double) {
+  double x;
+  asm volatile("ld.shared.f64 %0, [%1];" : "=d"(x) : "r"(a));
+  return x;
+}
+
 template <typename T> struct Vec16;
 template <> struct Vec16<float> {
   using type = float4;
@@ -1313,16 +1337,50 @@ __global__ void __launch_bounds__(INTERP_TILE_THREADS)
       }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < np; i += blockDim.x) {
-      const int p = p0 + i;
-      const int j = L.perm[p];
+    // per point: weights once per round, then the tile rows at constant offsets
+    // from a 32-bit shared address (3D)
+    constexpr uint32_t CS = sizeof(cplx<T>);
+    const uint32_t tile_s = smem_addr(tile), kz_s = smem_addr(kzs);
+    const uint32_t rs = (uint32_t)tx * CS, ps = (uint32_t)txy * CS;
+    // (3D: the next point's index and coordinates are prefetched; in 2D that
+    // measured slower with many transforms per round)
+    int i = threadIdx.x;
+    int jn = 0;
+    T ln0 = T(0), ln1 = T(0), ln2 = T(0);
+    if (DIM == 3 && i < np) {
+      jn = L.perm[p0 + i];
+      ln0 = L.loc[0][p0 + i];
+      ln1 = L.loc[1][p0 + i];
+      ln2 = L.loc[DIM - 1][p0 + i];
+    }
+    for (; i < np; i += blockDim.x) {
+      int j;
+      T l0, l1, l2;
+      if constexpr (DIM == 3) {
+        j = jn;
+        l0 = ln0;
+        l1 = ln1;
+        l2 = ln2;
+        const int inext = i + blockDim.x;
+        if (inext < np) {
+          jn = L.perm[p0 + inext];
+          ln0 = L.loc[0][p0 + inext];
+          ln1 = L.loc[1][p0 + inext];
+          ln2 = L.loc[2][p0 + inext];
+        }
+      } else {
+        j = L.perm[p0 + i];
+        l0 = L.loc[0][p0 + i];
+        l1 = L.loc[1][p0 + i];
+        l2 = T(0);
+      }
       T kx[NS], ky[NS];
-      const int sx = point_weights<T, NS>(L.loc[0][p], L.bin[0], K, kx);
-      const int sy = point_weights<T, NS>(L.loc[1][p], L.bin[1], K, ky);
+      const int sx = point_weights<T, NS>(l0, L.bin[0], K, kx);
+      const int sy = point_weights<T, NS>(l1, L.bin[1], K, ky);
       int sz = 0;
       if constexpr (DIM == 3) {
         T kz[NS];
-        sz = point_weights<T, NS>(L.loc[2][p], L.bin[2], K, kz);
+        sz = point_weights<T, NS>(l2, L.bin[2], K, kz);
 #pragma unroll
         for (int cc = 0; cc < NS; ++cc) kzs[cc] = kz[cc]; // read back with a dynamic index
       }
@@ -1333,12 +1391,15 @@ __global__ void __launch_bounds__(INTERP_TILE_THREADS)
         pf = post[j];
         if (conj_post) pf.y = -pf.y;
       }
-      const int base = sz * txy + sy * tx + sx;
+      const uint32_t base_s = tile_s + (uint32_t)(sz * txy + sy * tx + sx) * CS;
 #pragma unroll 1
       for (int k = 0; k < nt; ++k) {
-        const cplx<T> *tl = tile + (size_t)k * cells + base;
+        const uint32_t tk = base_s + (uint32_t)(k * cells) * CS;
         T accr = T(0), acci = T(0);
         if constexpr (DIM == 2) {
+          // 2D: plain loads (the compiler interleaves them across the rows
+          // better than volatile ones when many transforms share a round)
+          const cplx<T> *tl = tile + (size_t)k * cells + (sy * tx + sx);
 #pragma unroll
           for (int bb = 0; bb < NS; ++bb) {
             T rr = T(0), ri = T(0);
@@ -1354,22 +1415,25 @@ __global__ void __launch_bounds__(INTERP_TILE_THREADS)
         } else {
 #pragma unroll 1
           for (int cc = 0; cc < NS; ++cc) {
-            const cplx<T> *tp = tl + cc * txy;
+            const uint32_t plane = tk + (uint32_t)cc * ps;
             T pr = T(0), pi = T(0);
 #pragma unroll
             for (int bb = 0; bb < NS; ++bb) {
+              const uint32_t row = plane + (uint32_t)bb * rs;
               T rr = T(0), ri = T(0);
 #pragma unroll
               for (int a = 0; a < NS; ++a) {
-                const cplx<T> g = tp[bb * tx + a];
-                rr = fma(g.x, kx[a], rr);
-                ri = fma(g.y, kx[a], ri);
+                T gx, gy;
+                lds_cplx(row + a * CS, gx, gy);
+                rr = fma(gx, kx[a], rr);
+                ri = fma(gy, kx[a], ri);
               }
               pr = fma(rr, ky[bb], pr);
               pi = fma(ri, ky[bb], pi);
             }
-            accr = fma(pr, kzs[cc], accr);
-            acci = fma(pi, kzs[cc], acci);
+            const T wz = lds_real(kz_s + (uint32_t)cc * (uint32_t)sizeof(T), T(0));
+            accr = fma(pr, wz, accr);
+            acci = fma(pi, wz, acci);
           }
         }
         cplx<T> r;
