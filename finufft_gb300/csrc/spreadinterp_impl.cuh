@@ -715,34 +715,57 @@ __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
   }
   if (cur >= 0) flush();
   __syncthreads();
-  // write back planes zlo..zhi: lanes cover (x, row) pairs
+  // write back planes zlo..zhi. Lanes take x units of two cells whose first
+  // global index is even, added with one 16-byte reduction (float: (re, im)
+  // of both cells) when that address is 16-byte aligned; edge cells, tiles
+  // wider than the grid and unaligned pairs go one by one
   cplx<T> *fwt = fw + (int64_t)tr * nf_total + goff;
   const int tx = G.t[0], ty = G.t[1], tz = G.t[2];
   const bool fits = tx <= L.nf[0] && ty <= L.nf[1] && tz <= L.nf[2] && NS <= 2 * L.nf[0] &&
                     NS <= 2 * L.nf[1] && NS <= 2 * L.nf[2];
+  const int par = G.org[0] & 1;         // unit u starts at tile x = 2u - par
+  const int nun = (tx + par + 1) >> 1;  // units covering x = 0 .. tx-1
   int txp = 1;
-  while (txp < tx && txp < 32) txp <<= 1;
+  while (txp < nun && txp < 32) txp <<= 1;
   const int rows_per = blockDim.x / txp;
   const int rows = ty * (zhi - zlo + 1);
   const int64_t plane = (int64_t)L.nf[0] * L.nf[1];
-  for (int x0 = 0; x0 < tx; x0 += txp) {
-    const int x = x0 + (threadIdx.x & (txp - 1));
-    const int gx = fits ? wrap_once(G.org[0] + x, L.nf[0]) : wrap_idx(G.org[0] + x, L.nf[0]);
+  for (int u0 = 0; u0 < nun; u0 += txp) {
+    const int u = u0 + (threadIdx.x & (txp - 1));
+    const int xa = 2 * u - par, xb = xa + 1; // the unit's cells (valid if in [0, tx))
+    const bool va = u < nun && xa >= 0, vb = u < nun && xb < tx;
+    const int gxa = va ? (fits ? wrap_once(G.org[0] + xa, L.nf[0]) : wrap_idx(G.org[0] + xa, L.nf[0])) : 0;
+    const int gxb = vb ? (fits ? wrap_once(G.org[0] + xb, L.nf[0]) : wrap_idx(G.org[0] + xb, L.nf[0])) : 0;
+    const bool pair = va && vb && gxb == gxa + 1 && sizeof(T) == 4;
     int r0 = threadIdx.x / txp;
     int y = r0 % ty, z = zlo + r0 / ty;
     const int dy = rows_per % ty, dz = rows_per / ty;
     for (; r0 < rows; r0 += rows_per) {
-      if (x < tx) {
-        const int sidx = z * Q + y * px + x;
-        cplx<T> v;
-        v.x = re[sidx];
-        v.y = im[sidx];
-        if (v.x != T(0) || v.y != T(0)) {
+      if (va || vb) {
+        const int sidx = z * Q + y * px;
+        cplx<T> a, b;
+        a.x = va ? re[sidx + xa] : T(0);
+        a.y = va ? im[sidx + xa] : T(0);
+        b.x = vb ? re[sidx + xb] : T(0);
+        b.y = vb ? im[sidx + xb] : T(0);
+        const bool nza = a.x != T(0) || a.y != T(0), nzb = b.x != T(0) || b.y != T(0);
+        if (nza || nzb) {
           const int gy = fits ? wrap_once(G.org[1] + y, L.nf[1]) : wrap_idx(G.org[1] + y, L.nf[1]);
           const int gz = fits ? wrap_once(G.org[2] + z, L.nf[2]) : wrap_idx(G.org[2] + z, L.nf[2]);
-          atomic_add_cplx_global(fwt + gx + (int64_t)L.nf[0] * gy + plane * gz, v);
+          cplx<T> *row = fwt + (int64_t)L.nf[0] * gy + plane * gz;
+          if constexpr (sizeof(T) == 4) {
+            // (16-byte alignment is checked: spread-only grids may have odd sizes)
+            if (pair && (reinterpret_cast<uintptr_t>(row + gxa) & 15u) == 0) {
+              atomicAdd(reinterpret_cast<float4 *>(row + gxa),
+                        make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y));
+              goto next_row;
+            }
+          }
+          if (va && nza) atomic_add_cplx_global(row + gxa, a);
+          if (vb && nzb) atomic_add_cplx_global(row + gxb, b);
         }
       }
+    next_row:
       y += dy;
       z += dz;
       if (y >= ty) {
