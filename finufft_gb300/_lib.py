@@ -54,7 +54,8 @@ class PlanInfo(Structure):
 class GbnufftOpts(Structure):
     """gbnufft_opts (include/gbnufft_ext.h)."""
 
-    _fields_ = [("planner", c_int), ("spread_variant", c_int), ("reserved", c_int * 14)]
+    _fields_ = [("planner", c_int), ("spread_variant", c_int), ("fft_prune", c_int),
+                ("reserved", c_int * 13)]
 
 
 class FinufftOpts(Structure):

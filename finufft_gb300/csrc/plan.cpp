@@ -106,6 +106,9 @@ template <typename T> Plan<T>::~Plan() {
   try {
     DeviceScope ds(opts.gpu_device_id);
     if (have_fft) cufftDestroy(fftplan);
+    if (fft_x) cufftDestroy(fft_x);
+    if (fft_rest0) cufftDestroy(fft_rest0);
+    if (fft_rest1) cufftDestroy(fft_rest1);
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
   } catch (...) {
@@ -281,6 +284,36 @@ template <typename T> void Plan<T>::make_fft() {
     GBN_THROW(r == CUFFT_ALLOC_FAILED ? FINUFFT_ERR_ALLOC : FINUFFT_ERR_CUDA_FAILURE, "cufft");
   }
   cufftSetStream(fftplan, stream);
+  if (dim >= 2 && ext.fft_prune == 1) make_pruned_fft();
+}
+
+// Pruned FFT: the retained modes use only the x columns [0, keep0) and
+// [nf0 - keep1, nf0), so after (type 1) or before (type 2) a full 1D pass
+// along x, the passes over y (and z) run on those columns alone.
+template <typename T> void Plan<T>::make_pruned_fft() {
+  const cufftType ty = std::is_same_v<T, float> ? CUFFT_C2C : CUFFT_Z2Z;
+  keep0 = ms[0] - ms[0] / 2;
+  keep1 = ms[0] / 2;
+  auto check = [](cufftResult r) {
+    if (r != CUFFT_SUCCESS)
+      GBN_THROW(r == CUFFT_ALLOC_FAILED ? FINUFFT_ERR_ALLOC : FINUFFT_ERR_CUDA_FAILURE, "cufft");
+  };
+  size_t work = 0;
+  long long nx[1] = {nf[0]};
+  check(cufftCreate(&fft_x));
+  check(cufftMakePlanMany64(fft_x, 1, nx, nx, 1, nf[0], nx, 1, nf[0], ty,
+                            (long long)nf[1] * nf[2] * batchsize, &work));
+  cufftSetStream(fft_x, stream);
+  long long nr[2];
+  for (int d = 1; d < dim; ++d) nr[d - 1] = nf[dim - d]; // slowest dimension first
+  auto rest = [&](cufftHandle *h, int cols) {
+    check(cufftCreate(h));
+    check(cufftMakePlanMany64(*h, dim - 1, nr, nr, nf[0], 1, nr, nf[0], 1, ty, cols, &work));
+    cufftSetStream(*h, stream);
+  };
+  rest(&fft_rest0, keep0);
+  if (keep1 > 0) rest(&fft_rest1, keep1);
+  pruned = true;
 }
 
 template <typename T> void Plan<T>::make_fseries() {
@@ -455,14 +488,34 @@ template <typename T> void Plan<T>::check_ready() const {
   }
 }
 
-template <typename T> void Plan<T>::fft(cplx<T> *data, int sign) {
+template <typename T> void Plan<T>::fft(cplx<T> *data, int sign, bool spread_first) {
   const int dir = sign > 0 ? CUFFT_INVERSE : CUFFT_FORWARD;
-  cufftResult r;
-  if constexpr (std::is_same_v<T, float>)
-    r = cufftExecC2C(fftplan, (cufftComplex *)data, (cufftComplex *)data, dir);
-  else
-    r = cufftExecZ2Z(fftplan, (cufftDoubleComplex *)data, (cufftDoubleComplex *)data, dir);
-  if (r != CUFFT_SUCCESS) GBN_THROW(FINUFFT_ERR_CUDA_FAILURE, "cufftExec");
+  auto exec = [&](cufftHandle h, cplx<T> *d) {
+    cufftResult r;
+    if constexpr (std::is_same_v<T, float>)
+      r = cufftExecC2C(h, (cufftComplex *)d, (cufftComplex *)d, dir);
+    else
+      r = cufftExecZ2Z(h, (cufftDoubleComplex *)d, (cufftDoubleComplex *)d, dir);
+    if (r != CUFFT_SUCCESS) GBN_THROW(FINUFFT_ERR_CUDA_FAILURE, "cufftExec");
+  };
+  if (!pruned) {
+    exec(fftplan, data);
+    return;
+  }
+  auto rest = [&]() {
+    for (int b = 0; b < batchsize; ++b) {
+      cplx<T> *g = data + (int64_t)b * nf_total;
+      exec(fft_rest0, g);
+      if (keep1 > 0) exec(fft_rest1, g + (nf[0] - keep1));
+    }
+  };
+  if (spread_first) {
+    exec(fft_x, data);
+    rest();
+  } else {
+    rest();
+    exec(fft_x, data);
+  }
 }
 
 // Type-1 pipeline on ntr transforms: spread -> FFT(sign) -> deconvolve.
@@ -482,7 +535,7 @@ void Plan<T>::run_type1(const cplx<T> *c, cplx<T> *fk, int ntr, int sign, const 
     launch_spread<T>(L, K, cb, pre, conj_pre, grid, nf_total, blk, scfg, stream);
     if (time_stages) GBN_CUDA(cudaEventRecord(ev[1], stream));
     if (opts.gpu_spreadinterponly) continue;
-    fft(fw.p, sign);
+    fft(fw.p, sign, true);
     if (time_stages) GBN_CUDA(cudaEventRecord(ev[2], stream));
     launch_deconv<T>(dim, ms, nf, opts.modeord, inv, fw.p, nf_total, fkb, blk, stream);
     if (time_stages) GBN_CUDA(cudaEventRecord(ev[3], stream));
@@ -505,7 +558,7 @@ void Plan<T>::run_type2(const cplx<T> *fk, cplx<T> *c, int ntr, int sign,
     if (!opts.gpu_spreadinterponly) {
       launch_amplify<T>(dim, ms, nf, opts.modeord, inv, fkb, fw.p, nf_total, blk, stream);
       if (time_stages) GBN_CUDA(cudaEventRecord(ev[1], stream));
-      fft(fw.p, sign);
+      fft(fw.p, sign, false);
       grid = fw.p;
     } else if (time_stages)
       GBN_CUDA(cudaEventRecord(ev[1], stream));

@@ -110,17 +110,27 @@ public:
 private:
   void choose_spread_config(bool user_method);
   void make_fft();
+  void make_pruned_fft();
   void make_fseries();
   void sort_points(int64_t M, const T *const xyz[3], const AxisMap ax[3]);
   void run_type1(const cplx<T> *c, cplx<T> *fk, int ntr, int sign, const cplx<T> *pre,
                  int conj_pre);
   void run_type2(const cplx<T> *fk, cplx<T> *c, int ntr, int sign, const cplx<T> *post,
                  int conj_post);
-  void fft(cplx<T> *data, int sign);
+  // FFT of the batch in place; spread_first: the type-1 order (the grid came
+  // from a spread, only the retained modes are read afterwards), else the
+  // type-2 order (only the retained modes are nonzero before it)
+  void fft(cplx<T> *data, int sign, bool spread_first);
   void check_ready() const;
 
   cufftHandle fftplan = 0;
   bool have_fft = false;
+  // pruned FFT (2D/3D): a batched 1D pass along x over all lines, and passes
+  // over the other dimensions on the x columns of the retained modes only
+  // (the two ranges [0, keep0) and [nf0 - keep1, nf0))
+  bool pruned = false;
+  cufftHandle fft_x = 0, fft_rest0 = 0, fft_rest1 = 0;
+  int keep0 = 0, keep1 = 0;
   DevArray<cplx<T>> fw;        // batchsize fine grids
   DevArray<T> invphihat[3];    // 1/phihat per dimension, nf/2+1 each
   DevArray<cplx<T>> t3pre;     // type 3 pre-phase, M

@@ -331,3 +331,30 @@ def test_edge_cases(oracle, ty):
             f = q.execute(_dev(fk)).cpu().numpy()
             ref = oracle.dirft2(_oracle_pts(pts), fk.ravel(), -1, nm[::-1])
         assert oracle.rel_l2(f, ref) < 1e-3
+
+
+@pytest.mark.parametrize("ty,nm", [(1, (24, 33)), (2, (24, 33)), (1, (10, 12, 15)),
+                                   (2, (10, 12, 15))])
+def test_fft_prune_matches_full_fft(oracle, ty, nm):
+    """gbnufft_opts.fft_prune: the FFT as an x pass plus passes over the other
+    dimensions on the retained modes' x columns (odd mode counts make the two
+    column ranges unequal) gives the full FFT's result."""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(70 + ty + len(nm))
+    M, ntr = 3000, 3
+    pts = rng.uniform(-np.pi, np.pi, (len(nm), M)).astype(np.float32)
+    outs = []
+    data = _cx(rng, (ntr, M) if ty == 1 else (ntr,) + nm)
+    for prune in (0, 1):
+        p = fg.Plan(ty, nm, n_trans=ntr, eps=1e-5, isign=1 if ty == 1 else -1, fft_prune=prune,
+                    gpu_maxbatchsize=2)
+        p.setpts(*[_dev(q) for q in pts])
+        outs.append(p.execute(_dev(data)).cpu().numpy())
+    assert oracle.rel_l2(outs[1], outs[0]) < 1e-6
+    xs = [q.astype(np.float64) for q in pts[::-1]]
+    if ty == 1:
+        ref = oracle.dirft1(xs, data[2], 1, nm[::-1]).reshape(nm)
+    else:
+        ref = oracle.dirft2(xs, data[2].ravel(), -1, nm[::-1])
+    assert oracle.rel_l2(outs[1][2].ravel(), ref.ravel()) < 2e-4
