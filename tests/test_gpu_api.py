@@ -358,3 +358,42 @@ def test_fft_prune_matches_full_fft(oracle, ty, nm):
     else:
         ref = oracle.dirft2(xs, data[2].ravel(), -1, nm[::-1])
     assert oracle.rel_l2(outs[1][2].ravel(), ref.ravel()) < 2e-4
+
+
+@pytest.mark.parametrize("ty", [1, 3])
+def test_repeated_setpts(oracle, ty):
+    """setpts called again on one plan with more, then fewer points (the sort
+    arrays grow, then are reused): each execute equals its direct sum; a graph
+    captured before the new setpts is dropped (graph_launch refuses)."""
+    import torch
+
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(80 + ty)
+    nm = (12, 10, 14)
+    s = torch.cuda.Stream()
+    kw = dict(eps=1e-5, isign=1, gpu_stream=s.cuda_stream)
+    p = fg.Plan(ty, nm if ty == 1 else 3, **kw)
+    for k, M in enumerate((5000, 60000, 100)):
+        pts = rng.uniform(-np.pi, np.pi, (3, M)).astype(np.float32)
+        c = _cx(rng, M)
+        extra = {}
+        if ty == 3:
+            tg = rng.uniform(-8, 8, (3, 300 + 100 * k)).astype(np.float32)
+            extra = dict(s=_dev(tg[0]), t=_dev(tg[1]), u=_dev(tg[2]))
+        p.setpts(*[_dev(q) for q in pts], **extra)
+        if k == 1:
+            with pytest.raises(fg.NufftError):
+                p.graph_launch()  # the graph captured for the previous points is gone
+        dc = _dev(c)
+        out = p.execute(dc)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().ravel()
+        xs = [q.astype(np.float64) for q in pts[::-1]]
+        if ty == 1:
+            ref = oracle.dirft1(xs, c, 1, nm[::-1])
+        else:
+            ref = oracle.dirft3(xs, c, 1, [q.astype(np.float64) for q in tg[::-1]])
+        assert oracle.rel_l2(got, ref) < 2e-4, M
+        if k == 0:
+            p.graph_capture(dc, out)
