@@ -397,3 +397,23 @@ def test_repeated_setpts(oracle, ty):
         assert oracle.rel_l2(got, ref) < 2e-4, M
         if k == 0:
             p.graph_capture(dc, out)
+
+
+def test_trim_scratch_then_setpts(oracle, engine):
+    """gbnufft_trim_scratch releases the setpts scratch pool; the next setpts
+    allocates again and the transform is unchanged; a bad device is an error."""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(90)
+    M, nm = 20000, (16, 16, 16)
+    pts = rng.uniform(-np.pi, np.pi, (3, M)).astype(np.float32)
+    c = _cx(rng, M)
+    p = fg.Plan(1, nm, eps=1e-5, isign=1)
+    p.setpts(*[_dev(q) for q in pts])
+    a = p.execute(_dev(c)).cpu().numpy()
+    assert engine.gbnufft_trim_scratch(0) == 0
+    p.setpts(*[_dev(q) for q in pts])
+    b = p.execute(_dev(c)).cpu().numpy()
+    # the sort is deterministic; atomics add in any order (float rounding)
+    assert oracle.rel_l2(b, a) < 1e-6
+    assert engine.gbnufft_trim_scratch(999) != 0
