@@ -510,6 +510,27 @@ def run_config(args):
         out.update({"workload": "3D type 2 FP32, 256^3 modes, M=1e8 clustered, tol 1e-5",
                     "value": M / (ms * 1e-3), "unit": "NU pts/s", "ms_per_step": ms,
                     "stage_ms": {"interp": st[0], "fft": st[1], "amplify": st[2]}})
+    elif args.config == "c3f64":
+        # the metric's workload in double precision at tol 1e-12 (ns = 13)
+        M = args.m
+        pts = clustered_points(M, 1234 + 3, rng_dev="cuda").to(torch.float64)
+        gd = torch.Generator(device="cuda").manual_seed(99)
+        c = torch.randn(M, 2, generator=gd, device="cuda", dtype=torch.float64).view(torch.complex128)[:, 0]
+        x, y, z = (pts[d].contiguous() for d in range(3))
+        p = fg.Plan(1, N_MODES, eps=1e-12, dtype="complex128", gpu_stream=stream.cuda_stream)
+        p.setpts(x, y, z)
+        f = torch.empty(N_MODES, dtype=torch.complex128, device=dev)
+        ms = _timed(lambda: p.execute(c, out=f), stream, min(args.steps, 3), min(args.warmup, 1))
+        p.stage_times(True)
+        p.execute(c, out=f)
+        torch.cuda.synchronize()
+        st = p.stage_times(True)
+        err = sampled_error(x, y, z, c, f, dev, nsample=32, seed=5)
+        info = p.info()
+        out.update({"workload": "3D type 1 FP64, 256^3 modes, M=1e8 clustered, tol 1e-12",
+                    "value": M / (ms * 1e-3), "unit": "NU pts/s", "ms_per_step": ms,
+                    "stage_ms": {"spread": st[0], "fft": st[1], "deconv": st[2]},
+                    "rel_l2_err_sampled": err, "ns": info.ns, "spread_variant": info.spread_variant})
     elif args.config == "c5":
         # 3D type 3: M = K = 1e7, sources in box (1,2,4), targets in box (200,100,50)
         M = K = 10_000_000
@@ -574,7 +595,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4_000_000)
     ap.add_argument("--err-modes", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c3t2", "c4", "c5"],
+    ap.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c3f64", "c3t2", "c4", "c5"],
                     help="c3 (default) is the metric line; the others print their own line")
     ap.add_argument("--nmodes", type=int, default=0, help="modes per side (profiling cases)")
     ap.add_argument("--bins", default="", help="bin sizes x,y,z (default: the planner's)")
