@@ -197,7 +197,11 @@ BatchPlan<T>::BatchPlan(int type_, int dim_, int nprob_, const int64_t *modes, i
       const int64_t m = d < dim ? modes[3 * p + d] : 1;
       if (m < 1 || m > (1 << 30)) GBN_THROW(FINUFFT_ERR_NDATA_NOTVALID, "modes");
       h.ms[d] = (int)m;
-      h.nf[d] = d < dim ? (int)fine_grid_len(m, opts.upsampfac, K.ns) : 1;
+      // grids on the size ladder: the FFTs of problems with equal grid shapes
+      // run as one batched cuFFT call, and thousands of distinct shapes would
+      // be launch-bound (a finer grid at the same kernel width only lowers
+      // the error)
+      h.nf[d] = d < dim ? (int)ladder_grid_len(fine_grid_len(m, opts.upsampfac, K.ns)) : 1;
       nfmax[d] = std::max(nfmax[d], h.nf[d]);
     }
   }

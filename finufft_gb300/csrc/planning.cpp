@@ -158,6 +158,16 @@ KernelChoice choose_kernel(double tol, double sigma, int kerevalmeth, int is_flo
   return {ns, beta};
 }
 
+int64_t ladder_grid_len(int64_t n) {
+  int64_t best = 0;
+  for (int64_t p2 = 8; best == 0 || p2 <= best; p2 *= 2) {
+    for (const int64_t v : {p2, p2 * 5 / 4, p2 * 3 / 2, p2 * 15 / 8})
+      if (v % 2 == 0 && v >= n && (best == 0 || v < best)) best = v;
+    if (p2 > (int64_t)1 << 40) break;
+  }
+  return best;
+}
+
 int64_t fine_grid_len(int64_t ms, double sigma, int ns)
 // src/cuda/fft.cu:166-179 (set_nf_type12): ceil(sigma*ms), at least 2*ns, then
 // rounded up to an even 2,3,5-smooth length.

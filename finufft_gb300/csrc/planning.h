@@ -28,6 +28,10 @@ double es_kernel(double x, int ns, double beta);
 
 // Fine grid length for a type 1/2 dimension with ms modes.
 int64_t fine_grid_len(int64_t ms, double sigma, int ns);
+// The smallest even size of the ladder 2^k * {1, 5/4, 3/2, 15/8} (5-smooth)
+// that is >= n: batches of many problem sizes then share few FFT shapes (at
+// most 25% more cells per dimension than n, four sizes per octave).
+int64_t ladder_grid_len(int64_t n);
 
 // Type-3 grid: given source half-width X and frequency half-width S.
 void type3_grid(double sigma, double X, double S, int ns, int64_t *nf, double *h,

@@ -1,6 +1,7 @@
 """GPU tests of uneven batches (cufinufft[f]_batch_*): many independent
 transforms with different mode counts and point counts, executed by single
-launches over all problems. Every problem must equal a plan of its own and
+launches over all problems. Every problem must agree with a plan of its own
+(to the tolerance: the batch rounds fine grids up to a size ladder) and with
 the FP64 direct sum within the requested tolerance."""
 import ctypes
 
@@ -88,7 +89,9 @@ def test_uneven_batch_matches_single_plans(oracle, engine, dim, ty, prec):
         if np.linalg.norm(ref) == 0:
             assert np.abs(got).max() == 0
             continue
-        assert oracle.rel_l2(got, ref) < (1e-5 if prec == "f" else 1e-12), p
+        # batched grids come from a size ladder (up to 25% finer than a single
+        # plan's), so the two approximations agree to about tol, not bitwise
+        assert oracle.rel_l2(got, ref) < (1e-5 if prec == "f" else 10 * tol), p
         if p < 3:  # and the truth, for a few problems
             if ty == 1:
                 tru = oracle.dirft1([pts[p][d] for d in range(dim)], cs[p], 1, modes[p])
