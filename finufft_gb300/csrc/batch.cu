@@ -206,7 +206,7 @@ BatchPlan<T>::BatchPlan(int type_, int dim_, int nprob_, const int64_t *modes, i
     }
   }
   S = spread_setup<T>(dim, K.ns, nfmax, opts, ext, false);
-  if (dim == 2 && S.cfg.variant != 2 && S.method == 2)
+  if (dim == 2 && S.cfg.variant != 1 && S.cfg.variant != 2 && S.method == 2)
     GBN_THROW(FINUFFT_ERR_INSUFFICIENT_SHMEM, "batched spreading needs the tiled kernel");
   if (S.method != 2) GBN_THROW(FINUFFT_ERR_INSUFFICIENT_SHMEM, "batched spreading needs tiles");
   if (dim == 3 && S.cfg.variant == 1) // the exclusive-warp tiles serve single problems only

@@ -38,14 +38,14 @@ template <typename T> size_t spread_tile3v_bytes(int ns, const int bin[3], int w
 }
 template size_t spread_tile3v_bytes<float>(int, const int[3], int);
 template size_t spread_tile3v_bytes<double>(int, const int[3], int);
-template <typename T> size_t spread_tile2m_bytes(int ns, const int bin[3]) {
+template <typename T> size_t spread_tile2m_bytes(int ns, const int bin[3], int warps) {
   const size_t tile = (2 * sizeof(T) * (size_t)tile_pitch_x(3, bin[0] + ns) * (bin[1] + ns) + 15) /
                       16 * 16;
   const size_t stage = (33 * (ns + 4 * ((ns + 3) / 4) + 2) * sizeof(T) + 33 * 4 + 15) / 16 * 16;
-  return tile + 8 * stage;
+  return tile + (size_t)warps * stage;
 }
-template size_t spread_tile2m_bytes<float>(int, const int[3]);
-template size_t spread_tile2m_bytes<double>(int, const int[3]);
+template size_t spread_tile2m_bytes<float>(int, const int[3], int);
+template size_t spread_tile2m_bytes<double>(int, const int[3], int);
 template size_t spread_tile3m_bytes<float>(int, const int[3], int);
 template size_t spread_tile3m_bytes<double>(int, const int[3], int);
 template size_t spread_tile3w_bytes<float>(int, const int[3]);

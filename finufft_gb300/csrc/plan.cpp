@@ -185,16 +185,20 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
   S.cfg.smem = S.method == 2 ? S.smem : 0;
   S.cfg.variant = 0;
   if (dim == 2 && S.method == 2) {
-    // 2D: 0 shared tile + per-point atomics (thread per point), 2 warp-aggregated
+    // 2D: 0 shared tile + per-point atomics (thread per point), 1 one warp per
+    // tile with same-cell runs added by plain read-modify-writes, 2 eight warps
+    // per tile with runs added by atomics
     int variant = ext.planner == 1 ? 0 : 2;
-    if (ext.spread_variant >= 0) variant = ext.spread_variant == 2 ? 2 : 0;
-    if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT")) variant = std::atoi(e) == 2 ? 2 : 0;
-    const size_t sm2 = spread_tile2m_bytes<T>(ns, bins);
-    if (variant == 2 && (sm2 > (size_t)limit || bins[0] + ns >= 65536 || bins[1] + ns >= 32768))
+    if (ext.spread_variant >= 0) variant = ext.spread_variant;
+    if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT")) variant = std::atoi(e);
+    if (variant < 0 || variant > 2) variant = 0;
+    const int warps2 = variant == 1 ? 1 : 8;
+    const size_t sm2 = spread_tile2m_bytes<T>(ns, bins, warps2);
+    if (variant >= 1 && (sm2 > (size_t)limit || bins[0] + ns >= 65536 || bins[1] + ns >= 32768))
       variant = 0;
-    if (variant == 2) {
-      S.cfg.variant = 2;
-      S.cfg.threads = 256;
+    if (variant >= 1) {
+      S.cfg.variant = variant;
+      S.cfg.threads = 32 * warps2;
       S.cfg.smem = sm2;
       S.smem = sm2;
     }

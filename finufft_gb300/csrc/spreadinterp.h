@@ -16,7 +16,7 @@ template <typename T> size_t spread_tile_smem(int dim, int ns, const int bin[3],
 // Shared-memory bytes of the exclusive-warp 3D spread (variant 1).
 template <typename T> size_t spread_tile3w_bytes(int ns, const int bin[3]);
 // Shared-memory bytes of the warp-aggregated 2D spread (variant 2, 8 warps).
-template <typename T> size_t spread_tile2m_bytes(int ns, const int bin[3]);
+template <typename T> size_t spread_tile2m_bytes(int ns, const int bin[3], int warps = 8);
 template <typename T> size_t spread_tile3v_bytes(int ns, const int bin[3], int warps);
 // Shared-memory bytes of the warp-aggregated 3D spread (variant 2).
 template <typename T> size_t spread_tile3m_bytes(int ns, const int bin[3], int warps);

@@ -992,7 +992,10 @@ template <typename T> __host__ __device__ constexpr size_t tile2m_bytes(int ns, 
   return (2 * sizeof(T) * (size_t)tile_pitch_x(3, bx + ns) * (by + ns) + 15) / 16 * 16;
 }
 
-template <typename T, int NS>
+// EXCL: one warp per block owns the tile, so a run is added with plain
+// read-modify-writes (shared f32 atomics are compare-and-swap loops); the 2D
+// tile is small enough (~12 KB at 32x32 bins) for many such blocks per SM.
+template <typename T, int NS, bool EXCL = false>
 __global__ void __launch_bounds__(256)
     spread_tile2m_kernel(PointLayout<T> L0, KernelShape<T> K, const cplx<T> *__restrict__ c,
                          const cplx<T> *__restrict__ pre, int conj_pre,
@@ -1072,8 +1075,13 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
           for (int k = 0; k < NSLOT; ++k)
             if (ok[k]) {
-              atomicAdd(re + rb + off[k], ar[k]);
-              atomicAdd(im + rb + off[k], ai[k]);
+              if constexpr (EXCL) {
+                re[rb + off[k]] += ar[k];
+                im[rb + off[k]] += ai[k];
+              } else {
+                atomicAdd(re + rb + off[k], ar[k]);
+                atomicAdd(im + rb + off[k], ai[k]);
+              }
             }
         }
 #pragma unroll
@@ -1100,8 +1108,13 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int k = 0; k < NSLOT; ++k)
       if (ok[k]) {
-        atomicAdd(re + rb + off[k], ar[k]);
-        atomicAdd(im + rb + off[k], ai[k]);
+        if constexpr (EXCL) {
+          re[rb + off[k]] += ar[k];
+          im[rb + off[k]] += ai[k];
+        } else {
+          atomicAdd(re + rb + off[k], ar[k]);
+          atomicAdd(im + rb + off[k], ai[k]);
+        }
       }
   }
   __syncthreads();
@@ -1507,6 +1520,11 @@ template <typename T, int DIM> struct Dispatch {
       GBN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)cfg.smem));
       kern<<<grid, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
+    } else if (DIM == 2 && cfg.variant == 1) {
+      auto k1 = spread_tile2m_kernel<T, NS, true>;
+      GBN_CUDA(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)cfg.smem));
+      k1<<<grid, 32, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
     } else if (DIM == 2 && cfg.variant == 2) {
       auto k2 = spread_tile2m_kernel<T, NS>;
       GBN_CUDA(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -21,10 +21,10 @@ typedef struct gbnufft_opts {
   int planner;        /* 0: this engine's defaults; 1: the reference library's heuristic
                          (cuFINUFFT 2.6 bin sizes, method and subproblem size,
                          src/cuda/heuristics.cu:325-445) */
-  int spread_variant; /* -1 auto; 3D tiled spread: 0 shared tile with per-point
+  int spread_variant; /* -1 auto; tiled spread: 0 shared tile with per-point
                          atomics, 1 one warp per tile (no atomics, same-cell runs in
                          registers), 2 shared tile with same-cell register runs,
-                         3 as 2 with x-slack runs and vector staging (ns <= 8) */
+                         3 (3D) as 2 with x-slack runs and vector staging (ns <= 8) */
   int fft_prune;      /* 1: 2D/3D FFTs as a 1D pass along x plus passes over the other
                          dimensions on the x columns of the retained modes only
                          (measured slower than one cuFFT plan on GB300; default 0) */
