@@ -111,7 +111,12 @@ __global__ void bin_key_kernel(const T *__restrict__ x, const T *__restrict__ y,
                                const T *__restrict__ z, int M, AxisMap a0, AxisMap a1,
                                AxisMap a2, int nb0, int nb1, int cell_keys,
                                uint32_t *__restrict__ keys, T *__restrict__ rec) {
-  const uint32_t binvol = (uint32_t)a0.bin * (DIM > 1 ? a1.bin : 1) * (DIM > 2 ? a2.bin : 1);
+  // cell_keys: 0 bin only, 1 bin and cell, 2 bin and half cell (2 * cell + the
+  // fraction's half, per dimension; odd kernel widths start their support at
+  // the cell or the next one depending on that half)
+  const uint32_t hm = cell_keys == 2 ? 2u : 1u;
+  const uint32_t binvol = (uint32_t)a0.bin * hm * (DIM > 1 ? a1.bin * hm : 1) *
+                          (DIM > 2 ? a2.bin * hm : 1);
   // float coordinates on the identity map: single-precision fold and a
   // reciprocal division (exact below 2^20 cells after one correction step)
   const AxisMap am[3] = {a0, a1, a2};
@@ -141,9 +146,9 @@ __global__ void bin_key_kernel(const T *__restrict__ x, const T *__restrict__ y,
           r -= b;
         }
         key += ks * (uint32_t)q;
-        loc += ls * (uint32_t)r;
+        loc += ls * (hm == 2u ? 2u * (uint32_t)r + (f >= 0.5f ? 1u : 0u) : (uint32_t)r);
         ks *= (uint32_t)(d == 0 ? nb0 : nb1);
-        ls *= (uint32_t)b;
+        ls *= (uint32_t)b * hm;
         lc[d] = (T)__fadd_rn((float)r, f);
       }
       keys[i] = cell_keys ? key * binvol + loc : key;
@@ -155,20 +160,23 @@ __global__ void bin_key_kernel(const T *__restrict__ x, const T *__restrict__ y,
     int c;
     double f;
     T lc[4] = {T(0), T(0), T(0), T(0)};
+    auto cellkey = [&](int cm, double fr) {
+      return hm == 2u ? 2u * (uint32_t)cm + (fr >= 0.5 ? 1u : 0u) : (uint32_t)cm;
+    };
     fold_cell((double)x[i], a0, c, f);
     uint32_t key = (uint32_t)(c / a0.bin);
-    uint32_t loc = (uint32_t)(c - (c / a0.bin) * a0.bin);
+    uint32_t loc = cellkey(c - (c / a0.bin) * a0.bin, f);
     lc[0] = (T)((double)(c - (c / a0.bin) * a0.bin) + f);
     if (DIM > 1) {
       fold_cell((double)y[i], a1, c, f);
       key += (uint32_t)nb0 * (uint32_t)(c / a1.bin);
-      loc += (uint32_t)a0.bin * (uint32_t)(c - (c / a1.bin) * a1.bin);
+      loc += (uint32_t)a0.bin * hm * cellkey(c - (c / a1.bin) * a1.bin, f);
       lc[1] = (T)((double)(c - (c / a1.bin) * a1.bin) + f);
     }
     if (DIM > 2) {
       fold_cell((double)z[i], a2, c, f);
       key += (uint32_t)nb0 * (uint32_t)nb1 * (uint32_t)(c / a2.bin);
-      loc += (uint32_t)a0.bin * (uint32_t)a1.bin * (uint32_t)(c - (c / a2.bin) * a2.bin);
+      loc += (uint32_t)a0.bin * hm * (uint32_t)a1.bin * hm * cellkey(c - (c / a2.bin) * a2.bin, f);
       lc[2] = (T)((double)(c - (c / a2.bin) * a2.bin) + f);
     }
     keys[i] = cell_keys ? key * binvol + loc : key;

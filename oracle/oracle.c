@@ -229,15 +229,17 @@ void or_fold_many(int64_t n, const float *x, int nf, int f32, int *cell, double 
 /* one axis of a point: cell, and the bin-local coordinate in double (FP64
  * fold) or as the float the single-precision path stores */
 static void or_axis(double x, double shift, double scale, int nf, int bin, int f32, int *cell,
-                    double *local) {
+                    double *local, double *frac) {
   if (f32) {
     float f;
     or_fold_cell_f32((float)x, nf, cell, &f);
     *local = (double)((float)(*cell % bin) + f);
+    *frac = f;
   } else {
     double f;
     or_fold_cell(x, shift, scale, nf, cell, &f);
     *local = (double)(*cell - (*cell / bin) * bin) + f;
+    *frac = f;
   }
 }
 
@@ -253,7 +255,7 @@ static void or_axis(double x, double shift, double scale, int nf, int bin, int f
  * sort does for float plans). Returns 0. */
 int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *shift,
                 const double *scale, const int *nf, const int *bin, int32_t *perm,
-                void *loc, int loc_is_float, int float_inputs) {
+                void *loc, int loc_is_float, int float_inputs, int ns) {
   int nb[3] = {1, 1, 1};
   int bn[3] = {1, 1, 1};
   for (int d = 0; d < dim; ++d) {
@@ -261,8 +263,13 @@ int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *s
     bn[d] = bin[d];
   }
   const uint64_t nbins = (uint64_t)nb[0] * nb[1] * nb[2];
-  const uint64_t binvol = (uint64_t)bn[0] * bn[1] * bn[2];
+  uint64_t binvol = (uint64_t)bn[0] * bn[1] * bn[2];
   const int cell_keys = nbins * binvol <= 0xffffffffull;
+  /* odd kernel widths: half-cell keys (2 * cell + the fraction's half, per
+   * dimension) when they still fit 32 bits, as the engine's sort */
+  const int half = cell_keys && ns % 2 == 1 && nbins * (binvol << dim) <= 0xffffffffull;
+  const uint32_t hm = half ? 2u : 1u;
+  if (half) binvol <<= dim;
   const uint64_t nkeys = cell_keys ? nbins * binvol : nbins;
   int f32 = loc_is_float && float_inputs;
   for (int d = 0; d < dim; ++d)
@@ -273,12 +280,13 @@ int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *s
     uint32_t k = 0, stride = 1, lc = 0, lstride = 1;
     for (int d = 0; d < dim; ++d) {
       int c;
-      double l;
-      or_axis(coords[d][i], shift[d], scale[d], nf[d], bin[d], f32, &c, &l);
+      double l, fr;
+      or_axis(coords[d][i], shift[d], scale[d], nf[d], bin[d], f32, &c, &l, &fr);
       k += stride * (uint32_t)(c / bin[d]);
-      lc += lstride * (uint32_t)(c - (c / bin[d]) * bin[d]);
+      const uint32_t cm = (uint32_t)(c - (c / bin[d]) * bin[d]);
+      lc += lstride * (half ? 2u * cm + (fr >= 0.5 ? 1u : 0u) : cm);
       stride *= (uint32_t)nb[d];
-      lstride *= (uint32_t)bin[d];
+      lstride *= (uint32_t)bin[d] * hm;
     }
     key[i] = cell_keys ? k * (uint32_t)binvol + lc : k;
     cnt[key[i] + 1]++;
@@ -289,8 +297,8 @@ int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *s
     int64_t i = perm[p];
     for (int d = 0; d < dim; ++d) {
       int c;
-      double l;
-      or_axis(coords[d][i], shift[d], scale[d], nf[d], bin[d], f32, &c, &l);
+      double l, fr;
+      or_axis(coords[d][i], shift[d], scale[d], nf[d], bin[d], f32, &c, &l, &fr);
       if (loc_is_float) ((float *)loc)[(size_t)d * M + p] = (float)l;
       else ((double *)loc)[(size_t)d * M + p] = l;
     }

@@ -49,7 +49,7 @@ def lib():
         L.or_fine_grid.argtypes = [I64, d, i]
         L.or_fine_grid.restype = I64
         L.or_type3_grid.argtypes = [d, d, d, i, P]
-        L.or_bin_sort.argtypes = [i, I64, P, P, P, P, P, P, P, i, i]
+        L.or_bin_sort.argtypes = [i, I64, P, P, P, P, P, P, P, i, i, i]
         L.or_fold_many.argtypes = [I64, P, i, i, P, P]
         L.or_dirft1.argtypes = [i, I64, P, P, i, P, I64, P, P]
         L.or_dirft2.argtypes = [i, I64, P, i, P, P, I64, P, P]
@@ -251,8 +251,9 @@ def fold_positions(x, nf, f32):
     return cell[:len(x)], frac[:len(x)]
 
 
-def bin_sort(xs, nf, bins, shift=None, scale=None, loc_dtype=np.float32):
-    """Host replica of the device bin sort: (perm, loc[dim, M])."""
+def bin_sort(xs, nf, bins, shift=None, scale=None, loc_dtype=np.float32, ns=0):
+    """Host replica of the device bin sort: (perm, loc[dim, M]); ns = the plan's
+    kernel width (odd widths sort by half cell when the keys fit 32 bits)."""
     dim = len(xs)
     float_inputs = all(np.asarray(x).dtype == np.float32 for x in xs)
     xs = _coords(xs)
@@ -264,7 +265,8 @@ def bin_sort(xs, nf, bins, shift=None, scale=None, loc_dtype=np.float32):
     perm = np.zeros(max(M, 1), dtype=np.int32)
     loc = np.zeros((dim, max(M, 1)), dtype=loc_dtype)
     lib().or_bin_sort(dim, M, _ptrs(xs), _ptr(shift), _ptr(scale), _ptr(nfa), _ptr(ba),
-                      _ptr(perm), _ptr(loc), int(loc_dtype == np.float32), int(float_inputs))
+                      _ptr(perm), _ptr(loc), int(loc_dtype == np.float32), int(float_inputs),
+                      int(ns))
     return perm[:M], loc[:, :M]
 
 

@@ -125,19 +125,22 @@ def test_sort_bit_exact(oracle, dtype, dim):
     # a cluster: many points in one bin
     pts[:, 200:5200] = (0.01 * rng.standard_normal((dim, 5000))).astype(rdt)
     nm = CASES[dim][0]
-    plan = fg.Plan(1, nm, eps=1e-5 if rdt == np.float32 else 1e-10, dtype=dtype)
-    plan.setpts(*[_dev(p) for p in pts])
-    info = plan.info()
-    perm = np.zeros(M, dtype=np.int32)
-    loc = np.zeros(dim * M, dtype=rdt)
-    fn = getattr(plan._lib, plan._pfx + "_get_sort")
-    assert fn(plan._plan, perm.ctypes.data, loc.ctypes.data) == 0
-    # the coordinates as the engine received them (float32 for complex64 plans,
-    # which take the single-precision fold), fastest axis first
-    hperm, hloc = oracle.bin_sort([np.ascontiguousarray(p) for p in pts[::-1]],
-                                  list(info.nf)[:dim], list(info.bins)[:dim], loc_dtype=rdt)
-    np.testing.assert_array_equal(perm, hperm)
-    np.testing.assert_array_equal(loc.reshape(dim, M), hloc)
+    # even and odd kernel widths (odd ones sort by half cell)
+    for tol in ((1e-5, 1e-6) if rdt == np.float32 else (1e-10, 1e-12)):
+        plan = fg.Plan(1, nm, eps=tol, dtype=dtype)
+        plan.setpts(*[_dev(p) for p in pts])
+        info = plan.info()
+        perm = np.zeros(M, dtype=np.int32)
+        loc = np.zeros(dim * M, dtype=rdt)
+        fn = getattr(plan._lib, plan._pfx + "_get_sort")
+        assert fn(plan._plan, perm.ctypes.data, loc.ctypes.data) == 0
+        # the coordinates as the engine received them (float32 for complex64
+        # plans, which take the single-precision fold), fastest axis first
+        hperm, hloc = oracle.bin_sort([np.ascontiguousarray(p) for p in pts[::-1]],
+                                      list(info.nf)[:dim], list(info.bins)[:dim], loc_dtype=rdt,
+                                      ns=info.ns)
+        np.testing.assert_array_equal(perm, hperm)
+        np.testing.assert_array_equal(loc.reshape(dim, M), hloc)
 
 
 def _clustered(rng, dim, M, rdt):
