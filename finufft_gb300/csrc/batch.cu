@@ -47,7 +47,9 @@ template <typename T, int DIM>
 __global__ void batch_keys_kernel(const T *__restrict__ x, const T *__restrict__ y,
                                   const T *__restrict__ z, int Mtot, const int *__restrict__ poff,
                                   int nprob, const DevProb *__restrict__ P, uint32_t binvol,
-                                  uint32_t *__restrict__ keys) {
+                                  uint32_t ex, uint32_t *__restrict__ keys) {
+  // ex = 1: start-cell keys for odd kernel widths (the cell, or the next one
+  // when the fraction is at least one half; bin + 1 values per dimension)
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < Mtot; j += gridDim.x * blockDim.x) {
     const DevProb &pr = P[find_slot(poff, nprob, j)];
     const T *xyz[3] = {x, y, z};
@@ -59,9 +61,9 @@ __global__ void batch_keys_kernel(const T *__restrict__ x, const T *__restrict__
       fold_cell((double)xyz[d][j], AxisMap{0.0, 1.0, pr.nf[d], pr.bin[d]}, c, f);
       const int bc = c / pr.bin[d];
       bin += sb * (uint32_t)bc;
-      loc += sl * (uint32_t)(c - bc * pr.bin[d]);
+      loc += sl * ((uint32_t)(c - bc * pr.bin[d]) + (ex && f >= 0.5 ? 1u : 0u));
       sb *= (uint32_t)pr.nbin[d];
-      sl *= (uint32_t)pr.bin[d];
+      sl *= (uint32_t)pr.bin[d] + ex;
     }
     keys[j] = ((uint32_t)pr.binoff + bin) * binvol + loc;
   }
@@ -357,7 +359,11 @@ void BatchPlan<T>::setpts(const int64_t *npts, const T *x, const T *y, const T *
     GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "null coordinates");
   Mtot = (int)tot;
   upload_tables(npts);
-  const uint64_t binvol = (uint64_t)S.bins[0] * S.bins[1] * S.bins[2];
+  // odd kernel widths sort by the support's start cell when the keys fit
+  uint64_t binvol = (uint64_t)S.bins[0] * S.bins[1] * S.bins[2], sbinvol = 1;
+  for (int d = 0; d < dim; ++d) sbinvol *= (uint64_t)S.bins[d] + 1;
+  const uint32_t ex = K.ns % 2 == 1 && (uint64_t)nbins_total * sbinvol <= 0xffffffffull ? 1u : 0u;
+  if (ex) binvol = sbinvol;
   const uint64_t nkeys = (uint64_t)nbins_total * binvol;
   if (nkeys > 0xffffffffull) GBN_THROW(FINUFFT_ERR_MAXNALLOC, "batch too large for 32-bit keys");
   int keybits = 0;
@@ -369,9 +375,9 @@ void BatchPlan<T>::setpts(const int64_t *npts, const T *x, const T *y, const T *
   const T *ys = dim > 1 ? y : x, *zs = dim > 2 ? z : x;
   if (Mtot > 0) {
     const unsigned g = blocks_for(Mtot, 256);
-    if (dim == 1) batch_keys_kernel<T, 1><<<g, 256, 0, stream>>>(x, ys, zs, Mtot, d_poff.p, nprob, P, (uint32_t)binvol, keys.as<uint32_t>());
-    else if (dim == 2) batch_keys_kernel<T, 2><<<g, 256, 0, stream>>>(x, ys, zs, Mtot, d_poff.p, nprob, P, (uint32_t)binvol, keys.as<uint32_t>());
-    else batch_keys_kernel<T, 3><<<g, 256, 0, stream>>>(x, ys, zs, Mtot, d_poff.p, nprob, P, (uint32_t)binvol, keys.as<uint32_t>());
+    if (dim == 1) batch_keys_kernel<T, 1><<<g, 256, 0, stream>>>(x, ys, zs, Mtot, d_poff.p, nprob, P, (uint32_t)binvol, ex, keys.as<uint32_t>());
+    else if (dim == 2) batch_keys_kernel<T, 2><<<g, 256, 0, stream>>>(x, ys, zs, Mtot, d_poff.p, nprob, P, (uint32_t)binvol, ex, keys.as<uint32_t>());
+    else batch_keys_kernel<T, 3><<<g, 256, 0, stream>>>(x, ys, zs, Mtot, d_poff.p, nprob, P, (uint32_t)binvol, ex, keys.as<uint32_t>());
     GBN_LAUNCH_CHECK();
     stable_sort_by_bin(keys.as<uint32_t>(), Mtot, keybits, skeys.as<uint32_t>(), perm.p, stream);
     T *l0 = loc[0].p, *l1 = dim > 1 ? loc[1].p : l0, *l2 = dim > 2 ? loc[2].p : l0;

@@ -355,16 +355,19 @@ void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]
   for (int d = 0; d < dim; ++d) loc[d].resize(std::max<int64_t>(Mp, 1));
   const int nb = nbins[0] * nbins[1] * nbins[2];
   // keys carry the cell inside the bin when bins * bin volume fits 32 bits;
-  // for odd kernel widths the half cell too (2^dim more keys per bin), so
-  // points sharing their first support cell are adjacent after the sort
+  // for odd kernel widths the start cell of the support instead (the cell, or
+  // the next one when the fraction is at least one half: bin + 1 values per
+  // dimension), so points sharing their first support cell are adjacent
   const uint64_t binvol0 = (uint64_t)bins[0] * bins[1] * bins[2];
+  uint64_t sbinvol = 1;
+  for (int d = 0; d < dim; ++d) sbinvol *= (uint64_t)bins[d] + 1;
   int cell_keys = (uint64_t)nb * binvol0 <= 0xffffffffull ? 1 : 0;
-  // GBNUFFT_HALF_CELL=0 keeps whole-cell keys (tuning comparisons)
-  const char *hc = std::getenv("GBNUFFT_HALF_CELL");
-  if (cell_keys && K.ns % 2 == 1 && (uint64_t)nb * (binvol0 << dim) <= 0xffffffffull &&
+  // GBNUFFT_START_CELL_KEYS=0 keeps whole-cell keys (tuning comparisons)
+  const char *hc = std::getenv("GBNUFFT_START_CELL_KEYS");
+  if (cell_keys && K.ns % 2 == 1 && (uint64_t)nb * sbinvol <= 0xffffffffull &&
       !(hc && std::atoi(hc) == 0))
     cell_keys = 2;
-  const uint64_t binvol = cell_keys == 2 ? binvol0 << dim : binvol0;
+  const uint64_t binvol = cell_keys == 2 ? sbinvol : binvol0;
   cell_sorted = cell_keys ? 1 : 0;
   const uint64_t nkeys = cell_keys ? (uint64_t)nb * binvol : (uint64_t)nb;
   int keybits = 0;

@@ -111,12 +111,12 @@ __global__ void bin_key_kernel(const T *__restrict__ x, const T *__restrict__ y,
                                const T *__restrict__ z, int M, AxisMap a0, AxisMap a1,
                                AxisMap a2, int nb0, int nb1, int cell_keys,
                                uint32_t *__restrict__ keys, T *__restrict__ rec) {
-  // cell_keys: 0 bin only, 1 bin and cell, 2 bin and half cell (2 * cell + the
-  // fraction's half, per dimension; odd kernel widths start their support at
-  // the cell or the next one depending on that half)
-  const uint32_t hm = cell_keys == 2 ? 2u : 1u;
-  const uint32_t binvol = (uint32_t)a0.bin * hm * (DIM > 1 ? a1.bin * hm : 1) *
-                          (DIM > 2 ? a2.bin * hm : 1);
+  // cell_keys: 0 bin only, 1 bin and cell, 2 bin and start cell (the cell, or
+  // the next one when the fraction is at least one half: where an odd-width
+  // kernel's support starts), bin + 1 values per dimension
+  const uint32_t ex = cell_keys == 2 ? 1u : 0u;
+  const uint32_t binvol = ((uint32_t)a0.bin + ex) * (DIM > 1 ? (uint32_t)a1.bin + ex : 1u) *
+                          (DIM > 2 ? (uint32_t)a2.bin + ex : 1u);
   // float coordinates on the identity map: single-precision fold and a
   // reciprocal division (exact below 2^20 cells after one correction step)
   const AxisMap am[3] = {a0, a1, a2};
@@ -146,9 +146,9 @@ __global__ void bin_key_kernel(const T *__restrict__ x, const T *__restrict__ y,
           r -= b;
         }
         key += ks * (uint32_t)q;
-        loc += ls * (hm == 2u ? 2u * (uint32_t)r + (f >= 0.5f ? 1u : 0u) : (uint32_t)r);
+        loc += ls * ((uint32_t)r + (ex && f >= 0.5f ? 1u : 0u));
         ks *= (uint32_t)(d == 0 ? nb0 : nb1);
-        ls *= (uint32_t)b * hm;
+        ls *= (uint32_t)b + ex;
         lc[d] = (T)__fadd_rn((float)r, f);
       }
       keys[i] = cell_keys ? key * binvol + loc : key;
@@ -161,7 +161,7 @@ __global__ void bin_key_kernel(const T *__restrict__ x, const T *__restrict__ y,
     double f;
     T lc[4] = {T(0), T(0), T(0), T(0)};
     auto cellkey = [&](int cm, double fr) {
-      return hm == 2u ? 2u * (uint32_t)cm + (fr >= 0.5 ? 1u : 0u) : (uint32_t)cm;
+      return (uint32_t)cm + (ex && fr >= 0.5 ? 1u : 0u);
     };
     fold_cell((double)x[i], a0, c, f);
     uint32_t key = (uint32_t)(c / a0.bin);
@@ -170,13 +170,14 @@ __global__ void bin_key_kernel(const T *__restrict__ x, const T *__restrict__ y,
     if (DIM > 1) {
       fold_cell((double)y[i], a1, c, f);
       key += (uint32_t)nb0 * (uint32_t)(c / a1.bin);
-      loc += (uint32_t)a0.bin * hm * cellkey(c - (c / a1.bin) * a1.bin, f);
+      loc += ((uint32_t)a0.bin + ex) * cellkey(c - (c / a1.bin) * a1.bin, f);
       lc[1] = (T)((double)(c - (c / a1.bin) * a1.bin) + f);
     }
     if (DIM > 2) {
       fold_cell((double)z[i], a2, c, f);
       key += (uint32_t)nb0 * (uint32_t)nb1 * (uint32_t)(c / a2.bin);
-      loc += (uint32_t)a0.bin * hm * (uint32_t)a1.bin * hm * cellkey(c - (c / a2.bin) * a2.bin, f);
+      loc += ((uint32_t)a0.bin + ex) * ((uint32_t)a1.bin + ex) *
+             cellkey(c - (c / a2.bin) * a2.bin, f);
       lc[2] = (T)((double)(c - (c / a2.bin) * a2.bin) + f);
     }
     keys[i] = cell_keys ? key * binvol + loc : key;

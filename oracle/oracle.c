@@ -265,11 +265,14 @@ int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *s
   const uint64_t nbins = (uint64_t)nb[0] * nb[1] * nb[2];
   uint64_t binvol = (uint64_t)bn[0] * bn[1] * bn[2];
   const int cell_keys = nbins * binvol <= 0xffffffffull;
-  /* odd kernel widths: half-cell keys (2 * cell + the fraction's half, per
-   * dimension) when they still fit 32 bits, as the engine's sort */
-  const int half = cell_keys && ns % 2 == 1 && nbins * (binvol << dim) <= 0xffffffffull;
-  const uint32_t hm = half ? 2u : 1u;
-  if (half) binvol <<= dim;
+  /* odd kernel widths: start-cell keys (cell + 1 when the fraction is at
+   * least one half, so bin + 1 values per dimension) when they still fit 32
+   * bits, as the engine's sort */
+  uint64_t sbinvol = 1;
+  for (int d = 0; d < dim; ++d) sbinvol *= (uint64_t)bin[d] + 1;
+  const int half = cell_keys && ns % 2 == 1 && nbins * sbinvol <= 0xffffffffull;
+  const uint32_t ex = half ? 1u : 0u;
+  if (half) binvol = sbinvol;
   const uint64_t nkeys = cell_keys ? nbins * binvol : nbins;
   int f32 = loc_is_float && float_inputs;
   for (int d = 0; d < dim; ++d)
@@ -284,9 +287,9 @@ int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *s
       or_axis(coords[d][i], shift[d], scale[d], nf[d], bin[d], f32, &c, &l, &fr);
       k += stride * (uint32_t)(c / bin[d]);
       const uint32_t cm = (uint32_t)(c - (c / bin[d]) * bin[d]);
-      lc += lstride * (half ? 2u * cm + (fr >= 0.5 ? 1u : 0u) : cm);
+      lc += lstride * (cm + (half && fr >= 0.5 ? 1u : 0u));
       stride *= (uint32_t)nb[d];
-      lstride *= (uint32_t)bin[d] * hm;
+      lstride *= (uint32_t)bin[d] + ex;
     }
     key[i] = cell_keys ? k * (uint32_t)binvol + lc : k;
     cnt[key[i] + 1]++;
