@@ -92,6 +92,10 @@ template <typename T> struct PointLayout {
   const int *binprob = nullptr;
   // 1 when points inside a bin are also sorted by cell (x fastest, z slowest)
   int cell_sorted = 0;
+  // interpolation: when set (cplx<T>[ntr * M]), the tiled interpolation writes
+  // its results in sorted order here and a scatter pass per transform moves
+  // them to user order, so the scattered writes of one transform merge in L2
+  void *sorted_out = nullptr;
 };
 
 } // namespace gbn

@@ -135,6 +135,7 @@ private:
   DevArray<T> invphihat[3];    // 1/phihat per dimension, nf/2+1 each
   DevArray<cplx<T>> t3pre;     // type 3 pre-phase, M
   DevArray<cplx<T>> t3post;    // type 3 post factor, N
+  DevArray<cplx<T>> isort;     // type 2: sorted-order interpolation output, batchsize * M
   bool pts_set = false;
   SpreadConfig scfg{2, 256, 0};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
