@@ -55,7 +55,7 @@ class GbnufftOpts(Structure):
     """gbnufft_opts (include/gbnufft_ext.h)."""
 
     _fields_ = [("planner", c_int), ("spread_variant", c_int), ("fft_prune", c_int),
-                ("reserved", c_int * 13)]
+                ("spread_float_tile", c_int), ("reserved", c_int * 12)]
 
 
 class FinufftOpts(Structure):

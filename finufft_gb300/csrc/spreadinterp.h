@@ -9,6 +9,7 @@ struct SpreadConfig {
   int threads;      // CTA size
   size_t smem;      // dynamic shared memory bytes for method 2
   int variant = 0;  // 3D method 2: 0 shared tile + atomics, 1 exclusive warp tiles
+  int fixed = 0;    // 3D variant 3, single precision, ns <= 6: int32 fixed-point tile
 };
 
 // Shared-memory bytes of the tiled spread for a given tile and kernel width.

@@ -549,7 +549,15 @@ __device__ __forceinline__ double vget(const double2 &v, int u) { return u == 0 
 __device__ __forceinline__ float4 vmake(const float *e) { return make_float4(e[0], e[1], e[2], e[3]); }
 __device__ __forceinline__ double2 vmake(const double *e) { return make_double2(e[0], e[1]); }
 
-template <typename T, int NS>
+// FX (single precision): the tile holds int32 fixed point. The block first sums
+// |c_j| over its subproblem (S); every tile cell and every register run sum is
+// at most S (kernel values are at most 1), so values scaled by 2^30 / (1.01 S)
+// stay within int32, and the run flushes become native integer shared-memory
+// adds instead of compare-and-swap loops. The sums are exact; each flushed
+// value is rounded once to S * 2^-30 (about 22 significant bits for a dense
+// 4096-point subproblem, against 24 for a float tile rounded at every add).
+// A subproblem whose S is outside (2^-96, 2^100), inf or NaN keeps float atomics.
+template <typename T, int NS, bool FX = false>
 __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
     spread_tile3v_kernel(PointLayout<T> L0, KernelShape<T> K, const cplx<T> *__restrict__ c,
                          const cplx<T> *__restrict__ pre, int conj_pre,
@@ -607,6 +615,32 @@ __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
     }
   };
   fetch(w0 + lane);
+  float fsc = 1.f, finv = 1.f; // fixed point: tile cell = round(value * fsc)
+  bool fxb = false;
+  if constexpr (FX) {
+    __shared__ float s_sum[32];
+    float acc = 0.f;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+      const int j = L.perm[p0 + i];
+      cplx<T> v = ct[j];
+      if (pre) v = cmul_opt<T>(v, pre[j], conj_pre);
+      acc += sqrtf((float)v.x * (float)v.x + (float)v.y * (float)v.y);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) s_sum[warp] = acc;
+    __syncthreads();
+    float S = 0.f;
+    for (int w = 0; w < nwarp; ++w) S += s_sum[w];
+    const float bound = S * 1.01f;
+    // scale in (2^-70, 2^126): bounds outside (2^-96, 2^100), inf and NaN keep
+    // float atomics (an all-zero subproblem needs no scale)
+    fxb = bound == 0.f || (bound > 0x1p-96f && bound < 0x1p100f);
+    if (fxb && bound > 0.f) {
+      fsc = 0x1p30f / bound;
+      finv = 1.f / fsc;
+    }
+  }
   {
     uint4 *z4 = reinterpret_cast<uint4 *>(re + (size_t)zlo * Q);
     uint4 *z4i = reinterpret_cast<uint4 *>(im + (size_t)zlo * Q);
@@ -637,6 +671,17 @@ __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
   const T *kxl = kx + (lx + XS) * SK; // row lx - dx + XS is kxl - dx * SK
   auto flush = [&]() {
     const int rb = (cur >> 20) * Q + ((cur >> 10) & 1023) * px + (cur & 1023);
+    if constexpr (FX) {
+      if (fxb) {
+#pragma unroll
+        for (int r = 0; r < NR; ++r)
+          if (ok[r]) {
+            atomicAdd(reinterpret_cast<int *>(re + rb + off[r]), __float2int_rn(ar[r] * fsc));
+            atomicAdd(reinterpret_cast<int *>(im + rb + off[r]), __float2int_rn(ai[r] * fsc));
+          }
+        return;
+      }
+    }
 #pragma unroll
     for (int r = 0; r < NR; ++r)
       if (ok[r]) {
@@ -748,6 +793,14 @@ __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
         a.y = va ? im[sidx + xa] : T(0);
         b.x = vb ? re[sidx + xb] : T(0);
         b.y = vb ? im[sidx + xb] : T(0);
+        if constexpr (FX) {
+          if (fxb) {
+            a.x = (T)__float_as_int((float)a.x) * finv;
+            a.y = (T)__float_as_int((float)a.y) * finv;
+            b.x = (T)__float_as_int((float)b.x) * finv;
+            b.y = (T)__float_as_int((float)b.y) * finv;
+          }
+        }
         const bool nza = a.x != T(0) || a.y != T(0), nzb = b.x != T(0) || b.y != T(0);
         if (nza || nzb) {
           const int gy = fits ? wrap_once(G.org[1] + y, L.nf[1]) : wrap_idx(G.org[1] + y, L.nf[1]);
@@ -1509,6 +1562,8 @@ template <typename T, int DIM> struct Dispatch {
     } else if constexpr (DIM == 3) {
       if (NS <= 8 && cfg.variant == 3) {
         auto kv = spread_tile3v_kernel<T, (NS <= 8 ? NS : 8)>;
+        if constexpr (sizeof(T) == 4 && NS <= 6)
+          if (cfg.fixed) kv = spread_tile3v_kernel<T, NS, true>;
         GBN_CUDA(cudaFuncSetAttribute(kv, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)cfg.smem));
         kv<<<grid, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);

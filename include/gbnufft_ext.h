@@ -28,7 +28,12 @@ typedef struct gbnufft_opts {
   int fft_prune;      /* 1: 2D/3D FFTs as a 1D pass along x plus passes over the other
                          dimensions on the x columns of the retained modes only
                          (measured slower than one cuFFT plan on GB300; default 0) */
-  int reserved[13];
+  int spread_float_tile; /* 1: the 3D single-precision spread (variant 3) sums into a
+                         float tile with float atomics; 0 (default): for ns <= 6 it sums
+                         into an int32 fixed-point tile scaled per subproblem by the sum
+                         of its |c_j| (native integer adds; each flushed value rounded
+                         once to that sum times 2^-30) */
+  int reserved[12];
 } gbnufft_opts;
 
 typedef struct gbnufft_plan_info {

@@ -184,6 +184,63 @@ def test_spread_variants_3d(oracle, dtype, tol, bins):
     assert outs[3, "used"] == 3 or tol < 1e-6  # width 8 and below take variant 3
 
 
+@pytest.mark.parametrize("tol", [1e-3, 1e-5])
+@pytest.mark.parametrize("scale", [1.0, 1e25, 1e-20])
+def test_fixed_point_tile(oracle, tol, scale):
+    """single-precision 3D spread with the int32 fixed-point tile (the default
+    for ns <= 6) against the float tile and the FP64 direct sum, on clustered
+    points with a few strong sources among weak ones, at strength scales far
+    from 1 (the per-subproblem scale follows them)"""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(101)
+    nm, M, ntr = (16, 20, 24), 8000, 2
+    pts = _clustered(rng, 3, M, np.float32)
+    c = _cx(rng, (ntr, M), "complex64")
+    c[0, :50] *= 300.0  # a few strong sources among weak ones
+    c = (c * np.float32(scale)).astype(np.complex64)
+    outs = {}
+    for ft in (0, 1):
+        plan = fg.Plan(1, nm, n_trans=ntr, eps=tol, isign=1, spread_float_tile=ft)
+        assert plan.info().spread_variant == 3
+        plan.setpts(*[_dev(p) for p in pts])
+        outs[ft] = plan.execute(_dev(c)).cpu().numpy()
+    for k in range(ntr):
+        ref = oracle.dirft1(_oracle_pts(pts), c[k].astype(np.complex128) / scale, 1, nm[::-1])
+        got = outs[0][k].ravel().astype(np.complex128) / scale
+        assert oracle.rel_l2(got, ref) < 20 * tol, k
+        # the two tiles differ by float rounding only
+        alt = outs[1][k].ravel().astype(np.complex128) / scale
+        assert oracle.rel_l2(got, alt) < 3e-6, k
+
+
+def test_fixed_point_tile_nan_and_type3(oracle):
+    """a NaN strength reaches the output as with float atomics (its subproblem
+    keeps the float tile); type 3 spreads c times the pre-phase through the
+    fixed-point tile"""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(102)
+    M = 4000
+    pts = _clustered(rng, 3, M, np.float32)
+    c = _cx(rng, M, "complex64")
+    c[17] = np.nan
+    plan = fg.Plan(1, (12, 12, 12), eps=1e-5, isign=1)
+    plan.setpts(*[_dev(p) for p in pts])
+    f = plan.execute(_dev(c)).cpu().numpy()
+    assert np.isnan(f).any()
+    s = rng.uniform(-8, 8, (3, 600)).astype(np.float32)
+    c[17] = 1.0
+    outs = {}
+    for ft in (0, 1):
+        p3 = fg.Plan(3, 3, eps=1e-5, isign=1, spread_float_tile=ft)
+        p3.setpts(*[_dev(p) for p in pts], s=_dev(s[0]), t=_dev(s[1]), u=_dev(s[2]))
+        outs[ft] = p3.execute(_dev(c)).cpu().numpy().ravel()
+    ref = oracle.dirft3(_oracle_pts(pts), c.astype(np.complex128), 1, _oracle_pts(s))
+    assert oracle.rel_l2(outs[0], ref) < 2e-4
+    assert oracle.rel_l2(outs[0], outs[1]) < 3e-6
+
+
 @pytest.mark.parametrize("v", [2, 3])
 def test_spread_variants_type3(oracle, v):
     """type 3 (spread with the pre-phase factor) through the warp-aggregated variants"""
