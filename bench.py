@@ -266,7 +266,10 @@ def run_gpu(args):
     atom_per_launch = float(M) * nt * 2 * ns ** 3
     spread_ms = stb[0]
     achieved = atom_per_launch / (spread_ms * 1e-3)
-    peak = fg.smem_atomic_peak(dev.index) if hasattr(fg, "smem_atomic_peak") else None
+    # peak: the measured rate of the shared-memory add the kernel issues (native
+    # int32 for the fixed-point tile, else the f32 compare-and-swap loop)
+    fixed = bool(getattr(binfo, "spread_fixed", 0))
+    peak = fg.smem_atomic_peak(dev.index, i32=fixed)
     kname = {0: "spread_tile3_kernel", 1: "spread_tile3w_kernel", 2: "spread_tile3m_kernel",
              3: "spread_tile3v_kernel"}.get(binfo.spread_variant, "spread_global_kernel")
     # algorithmic HBM bytes of one spread launch (nt transforms): coordinates and
@@ -307,10 +310,13 @@ def run_gpu(args):
                 "api": "finufftf_execute (host pointers, pinned)", "rel_diff_vs_device_api": e2e_err},
         "gpu_launches": 2 * args.steps,
         "roofline": {"bound": "smem_atomic", "achieved": achieved / 1e9,
-                     "peak": (peak / 1e9) if peak else None, "unit": "G atomic f32 adds/s",
+                     "peak": (peak / 1e9) if peak else None,
+                     "unit": "G shared-memory adds/s (achieved: 2*ns^3 updates per point)",
                      "frac": (achieved / peak) if peak else None, "traffic": traffic,
                      "kernel": kname, "per_launch": atom_per_launch,
-                     "peak_source": "measured by gbnufft_smem_atomic_rate on this GPU"},
+                     "tile": "int32 fixed point" if fixed else "f32",
+                     "peak_source": ("measured by gbnufft_smem_atomic_rate_i32 on this GPU" if fixed
+                                     else "measured by gbnufft_smem_atomic_rate on this GPU")},
         "roofline_hbm": {"bound": "hbm", "achieved": hbm_ach / 1e9, "peak": hbm_peak,
                          "unit": "GB/s", "frac": (hbm_ach / 1e9 / hbm_peak) if hbm_peak else None,
                          "traffic": traffic, "kernel": kname,

@@ -32,10 +32,13 @@ def load_library():
     return _lib.load()
 
 
-def smem_atomic_peak(device=0):
-    """Measured conflict-free shared-memory f32 atomicAdd rate (ops/s)."""
+def smem_atomic_peak(device=0, i32=False):
+    """Measured conflict-free shared-memory atomicAdd rate (lane ops/s): f32,
+    or native int32 (the fixed-point tile's operation) with i32=True."""
     r = ctypes.c_double()
-    _check("smem_atomic_rate", _lib.load().gbnufft_smem_atomic_rate(device, ctypes.byref(r)))
+    lib = _lib.load()
+    fn = lib.gbnufft_smem_atomic_rate_i32 if i32 else lib.gbnufft_smem_atomic_rate
+    _check("smem_atomic_rate", fn(device, ctypes.byref(r)))
     return r.value
 
 

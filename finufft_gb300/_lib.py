@@ -47,7 +47,7 @@ class PlanInfo(Structure):
         ("nf", c_int * 3), ("bins", c_int * 3), ("method", c_int), ("nsub", c_int),
         ("M", c_int64), ("N", c_int64), ("spread_smem", c_size_t),
         ("horner_err", c_double), ("inner_nf", c_int * 3), ("spread_variant", c_int),
-        ("maxsubprobsize", c_int),
+        ("maxsubprobsize", c_int), ("spread_fixed", c_int),
     ]
 
 
@@ -150,6 +150,8 @@ def _declare(lib):
     lib.gbnufft_default_opts.restype = None
     lib.gbnufft_smem_atomic_rate.argtypes = [c_int, POINTER(c_double)]
     lib.gbnufft_smem_atomic_rate.restype = c_int
+    lib.gbnufft_smem_atomic_rate_i32.argtypes = [c_int, POINTER(c_double)]
+    lib.gbnufft_smem_atomic_rate_i32.restype = c_int
     lib.gbnufft_trim_scratch.argtypes = [c_int]
     lib.gbnufft_trim_scratch.restype = c_int
     for pfx, real in (("finufft", c_double), ("finufftf", c_float)):

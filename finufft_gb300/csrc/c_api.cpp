@@ -140,6 +140,7 @@ template <typename T> int info_dev(void *p, gbnufft_plan_info *info) {
     info->horner_err = P.horner_err;
     info->spread_variant = P.spread_variant_in_use();
     info->maxsubprobsize = P.maxsub;
+    info->spread_fixed = P.spread_fixed_in_use();
   });
 }
 
@@ -303,6 +304,14 @@ int gbnufft_smem_atomic_rate(int device, double *rate) {
     if (!rate) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "rate");
     gbn::DeviceScope ds(device);
     *rate = gbn::smem_atomic_rate(device);
+  });
+}
+
+int gbnufft_smem_atomic_rate_i32(int device, double *rate) {
+  return guarded([&] {
+    if (!rate) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "rate");
+    gbn::DeviceScope ds(device);
+    *rate = gbn::smem_atomic_rate(device, true);
   });
 }
 

@@ -346,22 +346,24 @@ void launch_t3_postfactor(int dim, const T *const stu[3], int N, const double C[
 }
 
 namespace {
-// Conflict-free shared-memory f32 atomicAdd loop: each warp adds into 32
-// consecutive words, so one instruction touches 32 distinct banks.
-__global__ void smem_atomic_probe(float *out, int iters) {
-  __shared__ float s[8192];
-  for (int i = threadIdx.x; i < 8192; i += blockDim.x) s[i] = 0.f;
+// Conflict-free shared-memory atomicAdd loop (f32, or int32 for the
+// fixed-point tile): each warp adds into 32 consecutive words, so one
+// instruction touches 32 distinct banks.
+template <typename U> __global__ void smem_atomic_probe(float *out, int iters) {
+  __shared__ U s[8192];
+  for (int i = threadIdx.x; i < 8192; i += blockDim.x) s[i] = U(0);
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const float v = 1.0f + threadIdx.x * 1e-3f;
+  const U v = (U)(1.0f + threadIdx.x * 1e-3f);
 #pragma unroll 4
   for (int it = 0; it < iters; ++it) atomicAdd(&s[(((it * 8 + w) * 32) & 8191) + lane], v);
   __syncthreads();
-  if (threadIdx.x == 0) out[blockIdx.x] = s[blockIdx.x & 8191];
+  if (threadIdx.x == 0) out[blockIdx.x] = (float)s[blockIdx.x & 8191];
 }
 } // namespace
 
-double smem_atomic_rate(int device) {
+double smem_atomic_rate(int device, bool i32) {
+  auto probe = i32 ? smem_atomic_probe<int> : smem_atomic_probe<float>;
   int sms = 0;
   GBN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   const int grid = sms * 8, iters = 1 << 14;
@@ -370,9 +372,9 @@ double smem_atomic_rate(int device) {
   cudaEvent_t a, b;
   GBN_CUDA(cudaEventCreate(&a));
   GBN_CUDA(cudaEventCreate(&b));
-  smem_atomic_probe<<<grid, 256>>>(d, iters); // warm-up
+  probe<<<grid, 256>>>(d, iters); // warm-up
   GBN_CUDA(cudaEventRecord(a));
-  smem_atomic_probe<<<grid, 256>>>(d, iters);
+  probe<<<grid, 256>>>(d, iters);
   GBN_CUDA(cudaEventRecord(b));
   GBN_CUDA(cudaEventSynchronize(b));
   float ms = 0;

@@ -42,6 +42,6 @@ void launch_t3_postfactor(int dim, const T *const stu[3], int N, const double C[
 
 // Measured conflict-free shared-memory f32 atomicAdd rate of a device
 // (lane operations per second): the denominator of the spreading roofline.
-double smem_atomic_rate(int device);
+double smem_atomic_rate(int device, bool i32 = false);
 
 } // namespace gbn

@@ -101,6 +101,7 @@ public:
   DevArray<int> sub_bin_, sub_start_, sub_count_;
   PointLayout<T> layout() const;
   int spread_variant_in_use() const { return scfg.variant; }
+  int spread_fixed_in_use() const { return scfg.variant == 3 ? scfg.fixed : 0; }
 
   // type 3 parameters (per dimension)
   double t3X[3] = {0, 0, 0}, t3C[3] = {0, 0, 0}, t3S[3] = {0, 0, 0}, t3D[3] = {0, 0, 0};

@@ -51,6 +51,7 @@ typedef struct gbnufft_plan_info {
   int inner_nf[3];     /* type 3: fine grid of the inner type-2 plan */
   int spread_variant;  /* 3D tiled spread variant in use */
   int maxsubprobsize;  /* points per subproblem in use */
+  int spread_fixed;    /* 1: the 3D spread sums into the int32 fixed-point tile */
 } gbnufft_plan_info;
 
 GBNUFFT_EXPORT void gbnufft_default_opts(gbnufft_opts *o);
@@ -105,6 +106,9 @@ GBNUFFT_BATCH_DECLS(cufinufftf, cufinufftf_batch_plan, float, cuFloatComplex)
 /* Measures the device's conflict-free shared-memory f32 atomicAdd rate
  * (lane operations per second), the peak the spreading kernels are held to. */
 GBNUFFT_EXPORT int gbnufft_smem_atomic_rate(int device, double *rate);
+/* The same for native int32 shared-memory atomicAdd (the fixed-point tile's
+ * operation). */
+GBNUFFT_EXPORT int gbnufft_smem_atomic_rate_i32(int device, double *rate);
 
 /* Spread-only type 1 without device allocation (no counterpart in the
  * reference): grid[g] = sum_j c[j] phi(g - x_j) on the periodic grid of
