@@ -234,7 +234,8 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
         variant = 2;
       } else {
         S.cfg.variant = 3;
-        S.cfg.fixed = std::is_same_v<T, float> && ns <= 6 && ext.spread_float_tile != 1;
+        S.cfg.fixed = std::is_same_v<T, float> && ext.spread_float_tile != 1 &&
+                      (ns <= 6 || ext.spread_float_tile == 2);
         S.cfg.threads = 32 * w;
         S.cfg.smem = vsm;
         S.smem = vsm;

@@ -1562,7 +1562,7 @@ template <typename T, int DIM> struct Dispatch {
     } else if constexpr (DIM == 3) {
       if (NS <= 8 && cfg.variant == 3) {
         auto kv = spread_tile3v_kernel<T, (NS <= 8 ? NS : 8)>;
-        if constexpr (sizeof(T) == 4 && NS <= 6)
+        if constexpr (sizeof(T) == 4 && NS <= 8) // ns 7-8 only when asked (option 2)
           if (cfg.fixed) kv = spread_tile3v_kernel<T, NS, true>;
         GBN_CUDA(cudaFuncSetAttribute(kv, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)cfg.smem));

@@ -214,6 +214,25 @@ def test_fixed_point_tile(oracle, tol, scale):
         assert oracle.rel_l2(got, alt) < 3e-6, k
 
 
+def test_fixed_point_tile_wide(oracle):
+    """spread_float_tile=2 uses the fixed-point tile at widths 7 and 8 as well
+    (a speed/accuracy trade): still within the suite's bound of the FP64 sum"""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(103)
+    nm, M = (16, 20, 24), 8000
+    pts = _clustered(rng, 3, M, np.float32)
+    c = _cx(rng, M, "complex64")
+    ref = oracle.dirft1(_oracle_pts(pts), c.astype(np.complex128), 1, nm[::-1])
+    for tol, ns in ((1e-6, 7), (1.2e-7, 8)):
+        plan = fg.Plan(1, nm, eps=tol, isign=1, spread_float_tile=2)
+        plan.setpts(*[_dev(p) for p in pts])
+        info = plan.info()
+        assert info.ns == ns and info.spread_fixed == 1
+        got = plan.execute(_dev(c)).cpu().numpy().ravel()
+        assert oracle.rel_l2(got, ref) < 1e-5, ns
+
+
 def test_fixed_point_tile_nan_and_type3(oracle):
     """a NaN strength reaches the output as with float atomics (its subproblem
     keeps the float tile); type 3 spreads c times the pre-phase through the
