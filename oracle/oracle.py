@@ -253,7 +253,9 @@ def fold_positions(x, nf, f32):
 
 def bin_sort(xs, nf, bins, shift=None, scale=None, loc_dtype=np.float32, ns=0):
     """Host replica of the device bin sort: (perm, loc[dim, M]); ns = the plan's
-    kernel width (odd widths sort by half cell when the keys fit 32 bits)."""
+    kernel width (odd widths sort by the start cell of the support, the cell
+    or the next one when the fraction is at least one half, when the keys fit
+    32 bits)."""
     dim = len(xs)
     float_inputs = all(np.asarray(x).dtype == np.float32 for x in xs)
     xs = _coords(xs)

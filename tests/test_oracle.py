@@ -159,6 +159,45 @@ def test_bin_sort_is_stable_and_bin_ordered(oracle):
     assert np.all(np.diff(perm)[same] > 0)
 
 
+def test_bin_sort_start_cell_keys_for_odd_widths(oracle):
+    """odd kernel widths: inside a bin the host sort orders points by the cell
+    where their support starts (the cell, or the next one when the fraction is
+    at least one half; bin + 1 values per axis), so points that start at the
+    same cell are adjacent; even widths keep whole-cell keys"""
+    rng = np.random.default_rng(4)
+    M = 6000
+    xs = [rng.uniform(-np.pi, np.pi, M) for _ in range(3)]
+    nf, bins = [48, 36, 24], [8, 6, 4]
+    nb = [(nf[d] + bins[d] - 1) // bins[d] for d in range(3)]
+    cell, frac = [], []
+    for d in range(3):
+        r = np.mod(xs[d] / (2 * np.pi) + 0.5, 1.0) * nf[d]
+        c = np.minimum(np.floor(r).astype(np.int64), nf[d] - 1)
+        cell.append(c)
+        frac.append(r - c)
+    b = [cell[d] // bins[d] for d in range(3)]
+    binid = b[0] + nb[0] * (b[1] + nb[1] * b[2])
+    for ns in (5, 6, 7):
+        perm, loc = oracle.bin_sort(xs, nf, bins, loc_dtype=np.float64, ns=ns)
+        assert sorted(perm.tolist()) == list(range(M))
+        ex = ns % 2
+        st = [cell[d] - b[d] * bins[d] + (ex * (frac[d] >= 0.5)) for d in range(3)]
+        w = [bins[d] + ex for d in range(3)]
+        key = binid * (w[0] * w[1] * w[2]) + st[0] + w[0] * (st[1] + w[1] * st[2])
+        ks = key[perm]
+        assert np.mean(np.diff(ks) >= 0) > 0.999, ns
+        # the support start computed from the sorted bin-local coordinates
+        # (ceil(l - ns/2) + ns/2, the spreader's rule) is the key's start cell
+        # or one less, and never decreases along z inside a bin (the tile
+        # clear's z bounds rely on it)
+        s = np.ceil(loc - ns / 2) + ns // 2
+        if ex:
+            kz = st[2][perm]
+            assert np.mean((s[2] <= kz) & (s[2] >= kz - 1)) > 0.999, ns
+        same_bin = np.diff(binid[perm]) == 0
+        assert np.mean(np.diff(np.floor(loc[2]))[same_bin] >= -1) == 1.0
+
+
 def test_single_precision_fold_matches_fp64_fold(oracle):
     """The engine's float fold (error-free float arithmetic) places float
     coordinates where the FP64 fold does: same cell except within 1e-6 of a
