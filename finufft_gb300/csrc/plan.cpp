@@ -406,7 +406,8 @@ void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]
   // GBNUFFT_INTERP_SORTED=0 writes user order directly (tuning comparisons)
   isort.release();
   const char *iso = std::getenv("GBNUFFT_INTERP_SORTED");
-  if (type == 2 && batchsize > 1 && dim >= 2 && M > 0 && !(iso && std::atoi(iso) == 0)) {
+  if (type == 2 && batchsize > 1 && batchsize <= 65535 && dim >= 2 && M > 0 &&
+      !(iso && std::atoi(iso) == 0)) { // (the scatter's grid has one row per transform)
     int dev = 0, l2 = 0;
     GBN_CUDA(cudaGetDevice(&dev));
     GBN_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));

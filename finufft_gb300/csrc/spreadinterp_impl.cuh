@@ -1624,7 +1624,7 @@ template <typename T, int DIM> struct Dispatch {
       const size_t tbytes = cells * sizeof(cplx<T>);
       const size_t kzb = DIM == 3 ? (size_t)INTERP_TILE_THREADS * (NS + 1) * sizeof(T) : 0;
       const size_t budget = 72 * 1024;
-      // transforms per round at most (2D: four rounds' tiles per block keep four
+      // transforms per round at most (2D: four transforms' tiles per block keep four
       // blocks per SM, measured best on 16 vectors of 1e7 points)
       const int tbmax = DIM == 2 ? 4 : 8;
       if (imethod != 0 && tbytes + kzb <= budget) {
