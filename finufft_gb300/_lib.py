@@ -47,7 +47,7 @@ class PlanInfo(Structure):
         ("nf", c_int * 3), ("bins", c_int * 3), ("method", c_int), ("nsub", c_int),
         ("M", c_int64), ("N", c_int64), ("spread_smem", c_size_t),
         ("horner_err", c_double), ("inner_nf", c_int * 3), ("spread_variant", c_int),
-        ("maxsubprobsize", c_int), ("spread_fixed", c_int),
+        ("maxsubprobsize", c_int), ("spread_fixed", c_int), ("kernel_form", c_int),
     ]
 
 
@@ -55,7 +55,8 @@ class GbnufftOpts(Structure):
     """gbnufft_opts (include/gbnufft_ext.h)."""
 
     _fields_ = [("planner", c_int), ("spread_variant", c_int), ("fft_prune", c_int),
-                ("spread_float_tile", c_int), ("reserved", c_int * 12)]
+                ("spread_float_tile", c_int), ("kernel_form", c_int), ("kerformula", c_int),
+                ("reserved", c_int * 10)]
 
 
 class FinufftOpts(Structure):
@@ -154,6 +155,11 @@ def _declare(lib):
     lib.gbnufft_smem_atomic_rate_i32.restype = c_int
     lib.gbnufft_trim_scratch.argtypes = [c_int]
     lib.gbnufft_trim_scratch.restype = c_int
+    lib.gbnufft_kernel_choice.argtypes = [c_double, c_double, c_int, c_int, c_int, c_int, c_int,
+                                          POINTER(c_int), POINTER(c_double)]
+    lib.gbnufft_kernel_choice.restype = c_int
+    lib.gbnufft_kernel_eval.argtypes = [c_int, c_int, c_double, c_int64, c_void_p, c_void_p]
+    lib.gbnufft_kernel_eval.restype = c_int
     for pfx, real in (("finufft", c_double), ("finufftf", c_float)):
         f = getattr(lib, pfx + "_makeplan")
         f.argtypes = [c_int, c_int, i64p, c_int, c_int, real, POINTER(c_void_p),

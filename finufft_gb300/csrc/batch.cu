@@ -188,9 +188,15 @@ BatchPlan<T>::BatchPlan(int type_, int dim_, int nprob_, const int64_t *modes, i
   DeviceScope ds(opts.gpu_device_id);
   stream = (cudaStream_t)opts.gpu_stream;
   if (opts.upsampfac == 0.0) opts.upsampfac = 2.0;
-  const KernelChoice kc = choose_kernel(tol, opts.upsampfac, opts.gpu_kerevalmeth,
-                                        std::is_same_v<T, float>, 0, opts.debug);
-  build_kernel_shape<T>(kc.ns, kc.beta, opts.gpu_kerevalmeth == 1, tol, &K);
+  const int form = plan_kernel_form(ext, opts);
+  const KernelChoice kc =
+      form == KERNEL_PSWF
+          ? choose_kernel_pswf(tol, opts.upsampfac, dim, type, std::is_same_v<T, float>,
+                               ext.kerformula, 0, opts.debug)
+          : choose_kernel(tol, opts.upsampfac, opts.gpu_kerevalmeth, std::is_same_v<T, float>,
+                          0, opts.debug);
+  build_kernel_shape<T>(make_kernel_fn(form, kc.ns, kc.beta), opts.gpu_kerevalmeth == 1, tol,
+                        &K);
   probs.resize(nprob);
   int nfmax[3] = {1, 1, 1};
   for (int p = 0; p < nprob; ++p) {
@@ -249,7 +255,7 @@ BatchPlan<T>::BatchPlan(int type_, int dim_, int nprob_, const int64_t *modes, i
   fw.resize((size_t)std::max<int64_t>(grid_total, 1));
   // 1/phihat per distinct grid length, shared by the problems that use it
   QuadNodes Qn;
-  Qn.q = kernel_ft_nodes(K.ns, (double)K.beta, 3.0, Qn.z, Qn.f);
+  Qn.q = kernel_ft_nodes(make_kernel_fn(K.form, K.ns, (double)K.beta), 3.0, Qn.z, Qn.f);
   std::map<int, int> invat;
   int invlen = 0;
   for (int p = 0; p < nprob; ++p)

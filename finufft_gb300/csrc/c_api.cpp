@@ -12,6 +12,7 @@
 #include "finufft.h"
 #include "gbnufft_ext.h"
 #include "plan.h"
+#include "planning.h"
 #include "sort.h"
 
 using gbn::Plan;
@@ -141,6 +142,7 @@ template <typename T> int info_dev(void *p, gbnufft_plan_info *info) {
     info->spread_variant = P.spread_variant_in_use();
     info->maxsubprobsize = P.maxsub;
     info->spread_fixed = P.spread_fixed_in_use();
+    info->kernel_form = P.K.form;
   });
 }
 
@@ -296,6 +298,31 @@ int gbnufft_trim_scratch(int device) {
   return guarded([&] {
     gbn::DeviceScope ds(device);
     gbn::trim_scratch_pool();
+  });
+}
+
+int gbnufft_kernel_choice(double tol, double sigma, int dim, int type, int is_float, int form,
+                          int kerformula, int *ns, double *beta) {
+  return guarded([&] {
+    if (!ns || !beta) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "ns/beta");
+    const gbn::KernelChoice kc =
+        form == gbn::KERNEL_PSWF
+            ? gbn::choose_kernel_pswf(tol, sigma, dim, type, is_float, kerformula, 0, 0)
+            : gbn::choose_kernel(tol, sigma, 0, is_float, 0, 0);
+    *ns = kc.ns;
+    *beta = kc.beta;
+  });
+}
+
+int gbnufft_kernel_eval(int form, int ns, double beta, int64_t n, const double *x,
+                        double *out) {
+  return guarded([&] {
+    if (form != gbn::KERNEL_ES && form != gbn::KERNEL_PSWF)
+      GBN_THROW(FINUFFT_ERR_KERFORMULA_NOTVALID, "form");
+    if (ns < 2 || ns > gbn::MAX_NS || n < 0 || (n > 0 && (!x || !out)))
+      GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "ns/n");
+    const gbn::KernelFn phi = gbn::make_kernel_fn(form, ns, beta);
+    for (int64_t i = 0; i < n; ++i) out[i] = phi(x[i]);
   });
 }
 

@@ -48,15 +48,19 @@ struct Error {
   } while (0)
 #define GBN_LAUNCH_CHECK() GBN_CUDA(cudaGetLastError())
 
-// ES ("exponential of semicircle") kernel phi(x) = exp(beta*(sqrt(1-(2x/ns)^2)-1)),
-// |x| < ns/2, and its piecewise-polynomial (Horner) form: piece j covers
+// Kernel forms: the GPU library's ES ("exponential of semicircle") kernel
+// phi(x) = exp(beta*(sqrt(1-(2x/ns)^2)-1)) and the CPU library's prolate
+// spheroidal wave function phi(x) = psi_0^beta(2x/ns), both on |x| < ns/2.
+enum { KERNEL_ES = 1, KERNEL_PSWF = 2 };
+
+// The spreading kernel and its piecewise-polynomial (Horner) form: piece j covers
 // x in [-ns/2+j, -ns/2+j+1], written as a polynomial in u = 2*(x - piece start) - 1.
 // coef[k][j] is the coefficient of u^(ndeg-1-k) of piece j (highest degree first).
 template <typename T> struct KernelShape {
   int ns;
   int use_horner; // 1: Horner pieces, 0: direct exp(sqrt())
   int ncoef;      // number of Horner coefficients per piece
-  int pad_;
+  int form;       // KERNEL_ES or KERNEL_PSWF (PSWF: always Horner)
   T beta;
   T es_c; // (2/ns)^2
   T coef[MAX_HCOEF][MAX_NS];

@@ -93,10 +93,12 @@ int makeplan_host(int type, int dim, const int64_t *n_modes, int iflag, int ntr,
     co.gpu_maxbatchsize = fo.maxbatchsize > 0 ? fo.maxbatchsize
                                               : std::min(8, std::max(1, (ntr + 3) / 4));
     if (fo.spread_max_sp_size > 0) co.gpu_maxsubprobsize = fo.spread_max_sp_size;
-    // the CPU library accepts any sigma > 1: use direct kernel evaluation off the
-    // two sigmas the GPU interface reserves for its Horner option
-    if (fo.upsampfac != 0.0 && fo.upsampfac != 2.0 && fo.upsampfac != 1.25)
-      co.gpu_kerevalmeth = 0;
+    // the CPU library's kernel: the PSWF with its shape choice (any sigma > 1;
+    // the pieces are fitted for the sigma given), spread/interp-only included
+    gbnufft_opts ext;
+    gbnufft_default_opts(&ext);
+    ext.kernel_form = gbn::KERNEL_PSWF;
+    ext.kerformula = fo.spread_kerformula;
     int dev = 0;
     GBN_CUDA(cudaGetDevice(&dev));
     co.gpu_device_id = dev;
@@ -111,7 +113,7 @@ int makeplan_host(int type, int dim, const int64_t *n_modes, int iflag, int ntr,
     h->dim = dim;
     h->ntr = ntr;
     h->nmodes = m3[0] * m3[1] * m3[2];
-    h->plan.reset(new Plan<T>(type, dim, m3, iflag, ntr, (double)tol, co));
+    h->plan.reset(new Plan<T>(type, dim, m3, iflag, ntr, (double)tol, co, &ext));
     *out = h.release();
   });
 }

@@ -89,9 +89,11 @@ int spread_noalloc_f(int dim, const int64_t *n_grid, int64_t M, const float *x, 
     gbnufft_opts ext;
     gbnufft_default_opts(&ext);
     // kernel and tiling exactly as a spread-only type-1 plan with default options
+    // (a spread-only plan keeps the GPU library's ES kernel: its output is the
+    // raw spread, whose values depend on the kernel shape)
     const KernelChoice kc = choose_kernel(eps, 2.0, 1, 1, 1, 0);
     KernelShape<float> K;
-    build_kernel_shape<float>(kc.ns, kc.beta, 1, eps, &K);
+    build_kernel_shape<float>(make_kernel_fn(KERNEL_ES, kc.ns, kc.beta), 1, eps, &K);
     const SpreadSetup S = spread_setup<float>(dim, kc.ns, nf, opts, ext, false);
 
     Arena arena;

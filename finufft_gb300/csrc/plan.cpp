@@ -24,6 +24,25 @@ extern "C" void gbnufft_default_opts(gbnufft_opts *o) {
 
 namespace gbn {
 
+int plan_kernel_form(const gbnufft_opts &ext, const cufinufft_opts &opts)
+// gbnufft_opts.kernel_form 0 (auto): the CPU library's PSWF, except under the
+// reference-heuristic planner, with direct kernel evaluation (gpu_kerevalmeth
+// 0; ES is the only form with a closed-form value) and for spread- or
+// interpolation-only plans, which keep the GPU library's ES kernel.
+// 1: ES, 2: PSWF.
+{
+  if (ext.kernel_form == KERNEL_ES || ext.kernel_form == KERNEL_PSWF) return ext.kernel_form;
+  if (ext.kernel_form != 0) {
+    fprintf(stderr, "[gbnufft] invalid kernel_form %d (0 auto, 1 ES, 2 PSWF)\n", ext.kernel_form);
+    GBN_THROW(FINUFFT_ERR_KERFORMULA_NOTVALID, "kernel_form");
+  }
+  if (ext.planner == 1 || opts.gpu_kerevalmeth == 0) return KERNEL_ES;
+  // a spread/interpolation-only plan returns the raw spread (or reads a raw
+  // grid), whose values depend on the kernel shape: keep the GPU library's
+  if (opts.gpu_spreadinterponly) return KERNEL_ES;
+  return KERNEL_PSWF;
+}
+
 DeviceScope::DeviceScope(int dev) {
   GBN_CUDA(cudaGetDevice(&prev));
   if (dev != prev) {
@@ -64,6 +83,7 @@ Plan<T>::Plan(int type_, int dim_, const int64_t *modes_in, int iflag_, int ntra
   if (opts.gpu_method < 0 || opts.gpu_method > 4) GBN_THROW(FINUFFT_ERR_METHOD_NOTVALID, "method");
   if (opts.gpu_method == 4 && dim != 3) GBN_THROW(FINUFFT_ERR_METHOD_NOTVALID, "method 4 is 3D only");
   stream = (cudaStream_t)opts.gpu_stream;
+  const int form = plan_kernel_form(ext, opts);
   if (type == 3) opts.gpu_spreadinterponly = 1; // the outer type 1 only spreads
   else
     for (int d = 0; d < dim; ++d) ms[d] = (int)modes_in[d];
@@ -80,9 +100,14 @@ Plan<T>::Plan(int type_, int dim_, const int64_t *modes_in, int iflag_, int ntra
       opts.upsampfac = 1.25;
   }
   const bool is_float = std::is_same_v<T, float>;
-  const KernelChoice kc = choose_kernel(tol, opts.upsampfac, opts.gpu_kerevalmeth, is_float,
-                                        opts.gpu_spreadinterponly, opts.debug);
-  horner_err = build_kernel_shape<T>(kc.ns, kc.beta, opts.gpu_kerevalmeth == 1, tol, &K);
+  const KernelChoice kc =
+      form == KERNEL_PSWF
+          ? choose_kernel_pswf(tol, opts.upsampfac, dim, type, is_float, ext.kerformula,
+                               opts.gpu_spreadinterponly, opts.debug)
+          : choose_kernel(tol, opts.upsampfac, opts.gpu_kerevalmeth, is_float,
+                          opts.gpu_spreadinterponly, opts.debug);
+  horner_err = build_kernel_shape<T>(make_kernel_fn(form, kc.ns, kc.beta),
+                                     opts.gpu_kerevalmeth == 1, tol, &K);
   if (type != 3) {
     for (int d = 0; d < dim; ++d)
       nf[d] = opts.gpu_spreadinterponly ? ms[d]
@@ -324,7 +349,7 @@ template <typename T> void Plan<T>::make_pruned_fft() {
 
 template <typename T> void Plan<T>::make_fseries() {
   QuadNodes Q;
-  Q.q = kernel_ft_nodes(K.ns, (double)K.beta, 3.0, Q.z, Q.f);
+  Q.q = kernel_ft_nodes(make_kernel_fn(K.form, K.ns, (double)K.beta), 3.0, Q.z, Q.f);
   for (int d = 0; d < dim; ++d) {
     invphihat[d].resize((size_t)nf[d] / 2 + 1);
     launch_inv_fseries<T>(nf[d], Q, invphihat[d].p, stream);
@@ -482,7 +507,7 @@ void Plan<T>::setpts(int64_t Mp, const T *x, const T *y, const T *z, int64_t Np,
   double scale[3];
   for (int d = 0; d < 3; ++d) scale[d] = t3h[d] * t3gam[d];
   QuadNodes Q;
-  Q.q = kernel_ft_nodes(K.ns, (double)K.beta, 2.0, Q.z, Q.f);
+  Q.q = kernel_ft_nodes(make_kernel_fn(K.form, K.ns, (double)K.beta), 2.0, Q.z, Q.f);
   double Cphase[3] = {0, 0, 0};
   for (int d = 0; d < dim; ++d)
     if (std::isfinite(t3C[d])) Cphase[d] = t3C[d];

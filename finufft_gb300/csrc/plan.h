@@ -58,6 +58,9 @@ struct SpreadSetup {
   SpreadConfig cfg{2, 256, 0};
   int maxsub = 1024; // points per subproblem at most
 };
+// Kernel form of a plan (KERNEL_ES or KERNEL_PSWF) from the options.
+int plan_kernel_form(const gbnufft_opts &ext, const cufinufft_opts &opts);
+
 template <typename T>
 SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts &opts,
                          const gbnufft_opts &ext, bool user_method);

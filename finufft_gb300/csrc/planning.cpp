@@ -82,6 +82,105 @@ double es_kernel(double x, int ns, double beta) {
   return std::exp(beta * (std::sqrt(1.0 - z * z) - 1.0));
 }
 
+namespace {
+// Legendre coefficients of the prolate spheroidal wave function psi_0^c on
+// [-1, 1] (Bouwkamp's expansion; Xiao, Rokhlin & Yarvin, Inverse Problems 17
+// (2001) 805-838): in the basis of normalised even Legendre polynomials
+// sqrt(n + 1/2) P_n, n = 2k, the prolate operator
+// -d/dz (1 - z^2) d/dz + c^2 z^2 is symmetric tridiagonal, and psi_0 is the
+// eigenvector of its smallest eigenvalue. That eigenvalue is bracketed by
+// bisection on the Sturm sequence count; the eigenvector comes from inverse
+// iteration with the shift just below it, where the shifted matrix is
+// positive definite and the LDL^T recurrence needs no pivoting. Returns a[k],
+// the coefficient of P_{2k} (unnormalised: psi(z) = sum_k a[k] P_{2k}(z)).
+std::vector<double> pswf0_legendre(double c) {
+  const int K = (int)c + 40; // the coefficients decay super-exponentially past k ~ c/2
+  std::vector<double> d(K), e(K > 1 ? K - 1 : 1, 0.0);
+  for (int k = 0; k < K; ++k) {
+    const double n = 2.0 * k;
+    d[k] = n * (n + 1) + c * c * (2 * n * n + 2 * n - 1) / ((2 * n - 1) * (2 * n + 3));
+  }
+  for (int k = 0; k + 1 < K; ++k) {
+    const double n = 2.0 * k;
+    e[k] = c * c * (n + 1) * (n + 2) / ((2 * n + 3) * std::sqrt((2 * n + 1) * (2 * n + 5)));
+  }
+  // Gershgorin bounds of the smallest eigenvalue
+  double lo = d[0] - std::fabs(e[0]), hi = d[0] + std::fabs(e[0]);
+  for (int k = 1; k < K; ++k) {
+    const double r = std::fabs(e[k - 1]) + (k + 1 < K ? std::fabs(e[k]) : 0.0);
+    lo = std::min(lo, d[k] - r);
+  }
+  // number of eigenvalues below x (Sturm count of the LDL^T pivots of T - x)
+  auto below = [&](double x) {
+    int cnt = 0;
+    double q = d[0] - x;
+    if (q < 0) ++cnt;
+    for (int k = 1; k < K; ++k) {
+      if (q == 0.0) q = 1e-300;
+      q = d[k] - x - e[k - 1] * e[k - 1] / q;
+      if (q < 0) ++cnt;
+    }
+    return cnt;
+  };
+  for (int it = 0; it < 200 && hi - lo > 4e-16 * std::max(1.0, std::fabs(hi)); ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (below(mid) >= 1) hi = mid;
+    else lo = mid;
+  }
+  // inverse iteration on T - lo (positive definite: lo is below the eigenvalue)
+  std::vector<double> v(K, 1.0), piv(K), w(K);
+  for (int it = 0; it < 4; ++it) {
+    piv[0] = d[0] - lo;
+    w[0] = v[0];
+    for (int k = 1; k < K; ++k) {
+      const double l = e[k - 1] / std::max(piv[k - 1], 1e-300);
+      piv[k] = d[k] - lo - l * e[k - 1];
+      w[k] = v[k] - l * w[k - 1];
+    }
+    v[K - 1] = w[K - 1] / std::max(piv[K - 1], 1e-300);
+    for (int k = K - 2; k >= 0; --k) v[k] = (w[k] - e[k] * v[k + 1]) / std::max(piv[k], 1e-300);
+    double nrm = 0;
+    for (double t : v) nrm += t * t;
+    nrm = std::sqrt(nrm);
+    for (double &t : v) t /= nrm;
+  }
+  for (int k = 0; k < K; ++k) v[k] *= std::sqrt(2.0 * k + 0.5);
+  return v;
+}
+
+// sum_k a[k] P_{2k}(z) by the three-term Legendre recurrence
+double legendre_even_sum(const std::vector<double> &a, double z) {
+  double p0 = 1.0, p1 = z, s = a[0];
+  const int nmax = 2 * ((int)a.size() - 1);
+  for (int n = 1; n < nmax; ++n) {
+    const double p2 = ((2.0 * n + 1.0) * z * p1 - n * p0) / (n + 1.0);
+    p0 = p1;
+    p1 = p2;
+    if ((n + 1) % 2 == 0) s += a[(n + 1) / 2] * p1;
+  }
+  return s;
+}
+} // namespace
+
+KernelFn make_kernel_fn(int form, int ns, double beta) {
+  KernelFn f;
+  f.form = form;
+  f.ns = ns;
+  f.beta = beta;
+  if (form == KERNEL_PSWF) {
+    f.leg = pswf0_legendre(beta);
+    f.scale = 1.0 / legendre_even_sum(f.leg, 0.0);
+  }
+  return f;
+}
+
+double KernelFn::operator()(double x) const {
+  if (form != KERNEL_PSWF) return es_kernel(x, ns, beta);
+  const double z = 2.0 * x / ns;
+  if (std::fabs(z) > 1.0) return 0.0;
+  return scale * legendre_even_sum(leg, z);
+}
+
 KernelChoice choose_kernel(double tol, double sigma, int kerevalmeth, int is_float,
                            int spreadinterponly, int debug)
 // GPU kernel-shape rule of src/cuda/makeplan.cu:43-119 (setup_spreadinterp):
@@ -158,6 +257,45 @@ KernelChoice choose_kernel(double tol, double sigma, int kerevalmeth, int is_flo
   return {ns, beta};
 }
 
+KernelChoice choose_kernel_pswf(double tol, double sigma, int dim, int type, int is_float,
+                                int kerformula, int spreadinterponly, int debug)
+// The CPU library's kernel (src/common/kernel.cpp:79-146): the PSWF psi_0^beta
+// with the width law ns = ceil(ln(tolfac/tol) / (pi sqrt(1 - 1/sigma)) + 1),
+// tolfac = 0.18 * 1.4^(dim-1) * (1.4 for type 3), and the shape parameter of
+// kerformula 8 (the default; beta = pi ns (1 - 1/(2 sigma)) - 0.05), 7 (Beatty)
+// or 9 (least-squares fit in t = beta_cutoff / pi). The width is the larger of
+// that law and the GPU library's rule above, so the kernel is never narrower
+// than the reference GPU's at the same tolerance; clipped as above.
+{
+  if (kerformula != 0 && (kerformula < 7 || kerformula > 9)) {
+    fprintf(stderr, "[gbnufft] error: kerformula=%d is not a PSWF shape choice (0, 7, 8, 9)\n",
+            kerformula);
+    GBN_THROW(FINUFFT_ERR_KERFORMULA_NOTVALID, "kerformula");
+  }
+  // argument checks and the GPU width rule (kerevalmeth 0: any sigma is legal here,
+  // the PSWF is always evaluated from fitted pieces)
+  const KernelChoice g = choose_kernel(tol, sigma, 0, is_float, spreadinterponly, 0);
+  const double eps_mach = is_float ? (double)FLT_EPSILON : DBL_EPSILON;
+  const double t = std::max(tol, eps_mach);
+  const double tolfac = 0.18 * std::pow(1.4, dim - 1) * (type == 3 ? 1.4 : 1.0);
+  int ns = (int)std::ceil(std::log(tolfac / t) / (PI * std::sqrt(1.0 - 1.0 / sigma)) + 1.0);
+  ns = std::max(ns, g.ns);
+  ns = std::max(2, std::min(ns, is_float ? MAX_NS_FLOAT : MAX_NS));
+  const double cut = PI * ns * (1.0 - 1.0 / (2.0 * sigma));
+  double beta = cut - 0.05;
+  if (kerformula == 7) {
+    const double cb = ns == 2 ? 0.5 : 0.8;
+    beta = std::sqrt(cut * cut - cb / (PI * PI));
+  } else if (kerformula == 9) {
+    const double tt = cut / PI;
+    beta = ((-0.00149087 * tt + 0.0218459) * tt + 3.06269) * tt - 0.0365245;
+  }
+  if (debug)
+    printf("[gbnufft] PSWF kernel: tol=%.3g sigma=%.3g: ns=%d beta=%.4g\n", tol, sigma, ns,
+           beta);
+  return {ns, beta};
+}
+
 int64_t ladder_grid_len(int64_t n) {
   int64_t best = 0;
   for (int64_t p2 = 8; best == 0 || p2 <= best; p2 *= 2) {
@@ -214,14 +352,15 @@ void width_center(double lo, double hi, double *w, double *c)
   *c = cc;
 }
 
-int horner_fit(int ns, double beta, double target_err, int maxcoef, std::vector<double> &coef,
+int horner_fit(const KernelFn &phi, double target_err, int maxcoef, std::vector<double> &coef,
                double *maxerr_out)
-// Piecewise polynomial of the ES kernel: piece j of ns covers
+// Piecewise polynomial of the kernel phi: piece j of ns covers
 // x in [-ns/2 + j, -ns/2 + j + 1]; it is the Chebyshev interpolant of degree
 // d-1 at d first-kind points in u = 2(x - start) - 1, rewritten in monomials of u.
 // The degree grows until the sampled max error is below target_err.
 {
   const int nsample = 64;
+  const int ns = phi.ns;
   maxcoef = std::min(maxcoef, MAX_HCOEF);
   int d = std::min(maxcoef, ns + 2);
   for (;; ++d) {
@@ -233,7 +372,7 @@ int horner_fit(int ns, double beta, double target_err, int maxcoef, std::vector<
       std::vector<long double> a(d, 0.0L), fv(d);
       for (int i = 0; i < d; ++i) {
         long double th = (long double)PI * (i + 0.5L) / d;
-        fv[i] = es_kernel(xof((double)cosl(th)), ns, beta);
+        fv[i] = phi(xof((double)cosl(th)));
       }
       for (int m = 0; m < d; ++m) {
         long double s = 0;
@@ -258,7 +397,7 @@ int horner_fit(int ns, double beta, double target_err, int maxcoef, std::vector<
         double u = -1.0 + 2.0 * t / nsample;
         double p = 0.0;
         for (int k = 0; k < d; ++k) p = p * u + coef[(size_t)k * MAX_NS + j];
-        maxerr = std::max(maxerr, std::fabs(p - es_kernel(xof(u), ns, beta)));
+        maxerr = std::max(maxerr, std::fabs(p - phi(xof(u))));
       }
     }
     if (maxerr <= target_err || d >= maxcoef) {
@@ -268,30 +407,33 @@ int horner_fit(int ns, double beta, double target_err, int maxcoef, std::vector<
   }
 }
 
-int kernel_ft_nodes(int ns, double beta, double nodes_per_halfwidth, double *z, double *f)
+int kernel_ft_nodes(const KernelFn &phi, double nodes_per_halfwidth, double *z, double *f)
 // Quadrature for the kernel's Fourier transform, as in src/cuda/fft.cu:185-202
 // (type 1/2: q = 2 + 1.5 ns) and :144-157 (type 3: q = 2 + ns): Gauss-Legendre
 // with 2q nodes on [-1,1]; by symmetry of the kernel only q nodes are kept and
 // the integral is 2 sum_n f_n cos(k z_n) with z_n in grid units.
 {
-  const double J2 = ns / 2.0;
+  const double J2 = phi.ns / 2.0;
   const int q = (int)(2 + nodes_per_halfwidth * J2);
   std::vector<double> x(2 * q), w(2 * q);
   gauss_legendre(2 * q, x.data(), w.data());
   for (int n = 0; n < q; ++n) {
     z[n] = J2 * x[n];
-    f[n] = J2 * w[n] * es_kernel(z[n], ns, beta);
+    f[n] = J2 * w[n] * phi(z[n]);
   }
   return q;
 }
 
 template <typename T>
-double build_kernel_shape(int ns, double beta, int use_horner, double tol, KernelShape<T> *K) {
+double build_kernel_shape(const KernelFn &phi, int use_horner, double tol, KernelShape<T> *K) {
   std::memset(K, 0, sizeof(*K));
+  const int ns = phi.ns;
   K->ns = ns;
-  K->beta = (T)beta;
+  K->form = phi.form;
+  K->beta = (T)phi.beta;
   K->es_c = (T)(4.0 / (double(ns) * ns));
-  K->use_horner = use_horner ? 1 : 0;
+  // direct evaluation exists for the ES form only; the PSWF is always fitted
+  K->use_horner = (use_horner || phi.form == KERNEL_PSWF) ? 1 : 0;
   // pieces are fitted for any sigma; the reference only carries tables for
   // sigma 2 and 1.25, which the option check already enforces
   std::vector<double> coef;
@@ -299,7 +441,7 @@ double build_kernel_shape(int ns, double beta, int use_horner, double tol, Kerne
   const bool is_float = std::is_same_v<T, float>;
   const double target = std::max(1e-2 * tol, is_float ? 2e-7 : 4e-15);
   const int H = horner_len(ns);
-  const int ncoef = horner_fit(ns, beta, target, H, coef, &err);
+  const int ncoef = horner_fit(phi, target, H, coef, &err);
   K->ncoef = H;
   for (int k = 0; k < H; ++k)
     for (int j = 0; j < ns; ++j) {
@@ -308,7 +450,7 @@ double build_kernel_shape(int ns, double beta, int use_horner, double tol, Kerne
     }
   return err;
 }
-template double build_kernel_shape<float>(int, double, int, double, KernelShape<float> *);
-template double build_kernel_shape<double>(int, double, int, double, KernelShape<double> *);
+template double build_kernel_shape<float>(const KernelFn &, int, double, KernelShape<float> *);
+template double build_kernel_shape<double>(const KernelFn &, int, double, KernelShape<double> *);
 
 } // namespace gbn

@@ -35,13 +35,20 @@ typedef struct gbnufft_opts {
                          once to that sum times 2^-30); 2: the fixed-point tile for ns 7
                          and 8 too, faster but less accurate there (1e8 clustered points:
                          tol 1e-6 error 1.5e-6 -> 2.2e-6, tol 1.2e-7 4.2e-7 -> 2.1e-6) */
-  int reserved[12];
+  int kernel_form;    /* 0 auto: the CPU library's PSWF kernel (psi_0, width and shape of
+                         src/common/kernel.cpp:79-146, never narrower than the GPU rule)
+                         fitted by Horner pieces, except under planner 1 or
+                         gpu_kerevalmeth 0, which keep the GPU library's ES kernel;
+                         1: ES (src/cuda/makeplan.cu:43-119); 2: PSWF */
+  int kerformula;     /* PSWF shape parameter choice as finufft_opts.spread_kerformula:
+                         0 or 8 (default), 7, 9; other values are rejected */
+  int reserved[10];
 } gbnufft_opts;
 
 typedef struct gbnufft_plan_info {
   int type, dim, ntransf, batchsize;
   int ns;              /* kernel width */
-  double beta;         /* ES kernel shape */
+  double beta;         /* kernel shape parameter (ES beta or PSWF c) */
   double upsampfac;    /* sigma actually used */
   int nf[3];           /* fine grid (type 3: outer grid) */
   int bins[3];         /* bin size per dimension */
@@ -54,6 +61,7 @@ typedef struct gbnufft_plan_info {
   int spread_variant;  /* 3D tiled spread variant in use */
   int maxsubprobsize;  /* points per subproblem in use */
   int spread_fixed;    /* 1: the 3D spread sums into the int32 fixed-point tile */
+  int kernel_form;     /* 1 ES, 2 PSWF */
 } gbnufft_plan_info;
 
 GBNUFFT_EXPORT void gbnufft_default_opts(gbnufft_opts *o);
@@ -104,6 +112,20 @@ typedef struct cufinufftf_batch_s *cufinufftf_batch_plan;
   GBNUFFT_EXPORT int P##_batch_destroy(PLAN plan);
 GBNUFFT_BATCH_DECLS(cufinufft, cufinufft_batch_plan, double, cuDoubleComplex)
 GBNUFFT_BATCH_DECLS(cufinufftf, cufinufftf_batch_plan, float, cuFloatComplex)
+
+/* Host-only planning queries (no device work). kernel_choice: the kernel
+ * width ns and shape parameter beta a plan of this type and dimension picks at
+ * tol and upsampling factor sigma, for form 1 (the GPU library's ES rule,
+ * src/cuda/makeplan.cu:43-119) or 2 (the CPU library's PSWF,
+ * src/common/kernel.cpp:79-146, never narrower than the GPU rule).
+ * kernel_eval: the kernel's values at n offsets x (grid units; support
+ * |x| <= ns/2), ES exp(beta (sqrt(1 - (2x/ns)^2) - 1)) or PSWF
+ * psi_0^beta(2x/ns) / psi_0^beta(0), as the Horner pieces are fitted to. */
+GBNUFFT_EXPORT int gbnufft_kernel_choice(double tol, double sigma, int dim, int type,
+                                         int is_float, int form, int kerformula, int *ns,
+                                         double *beta);
+GBNUFFT_EXPORT int gbnufft_kernel_eval(int form, int ns, double beta, int64_t n,
+                                       const double *x, double *out);
 
 /* Measures the device's conflict-free shared-memory f32 atomicAdd rate
  * (lane operations per second), the peak the spreading kernels are held to. */

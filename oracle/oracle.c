@@ -387,19 +387,31 @@ void or_dirft3(int dim, int64_t M, const double *const *xyz, const double *c, in
   }
 }
 
-/* ------------------------------------------- ES spread / interp (FP64) ---- */
+/* ------------------------------------- GPU-rule spread / interp (FP64) ---- */
 
-/* Grid weights of one point along one axis with the ES kernel: first cell
+/* Grid weights of one point along one axis with the ES kernel (or a tabulated
+ * kernel, coef != NULL): first cell
  * (wrapped into [0,nf)) and ns kernel values, as the GPU library places a point
  * (include/cufinufft/spreadinterp.hpp:166-196) but from the engine's FP64 fold. */
 static void or_axis_es(double x, double shift, double scale, int nf, int ns, double beta,
-                       int *start, double *ker) {
+                       int ncoef, const double *coef, int *start, double *ker) {
   int c;
   double f;
   or_fold_cell(x, shift, scale, nf, &c, &f);
   double r = (double)c + f;
   double s = ceil(r - 0.5 * ns);
-  for (int j = 0; j < ns; ++j) ker[j] = or_es_kernel(s - r + j, ns, beta);
+  if (coef) {
+    /* tabulated kernel (the PSWF): piece j of the support holds cell j, all at
+     * the same local variable u = 2 (s - r + ns/2) - 1; coef[k*ns + j] is the
+     * coefficient of u^(ncoef-1-k) of piece j */
+    const double u = 2.0 * (s - r + 0.5 * ns) - 1.0;
+    for (int j = 0; j < ns; ++j) {
+      double v = 0.0;
+      for (int k = 0; k < ncoef; ++k) v = v * u + coef[k * ns + j];
+      ker[j] = v;
+    }
+  } else
+    for (int j = 0; j < ns; ++j) ker[j] = or_es_kernel(s - r + j, ns, beta);
   int st = (int)s % nf;
   if (st < 0) st += nf;
   *start = st;
@@ -408,13 +420,13 @@ static void or_axis_es(double x, double shift, double scale, int nf, int ns, dou
 /* grid[g] += sum_j c_j phi(g - r_j) over the periodic grid nf[0..dim) (x fastest). */
 void or_spread_es(int dim, int64_t M, const double *const *xyz, const double *shift,
                   const double *scale, const double *c, const int *nf, int ns, double beta,
-                  double *grid) {
+                  int ncoef, const double *coef, double *grid) {
   double ker[3][32];
   int st[3] = {0, 0, 0};
   const int n1 = dim > 1 ? ns : 1, n2 = dim > 2 ? ns : 1;
   for (int64_t j = 0; j < M; ++j) {
     for (int d = 0; d < dim; ++d)
-      or_axis_es(xyz[d][j], shift[d], scale[d], nf[d], ns, beta, &st[d], ker[d]);
+      or_axis_es(xyz[d][j], shift[d], scale[d], nf[d], ns, beta, ncoef, coef, &st[d], ker[d]);
     for (int cz = 0; cz < n2; ++cz) {
       int64_t gz = dim > 2 ? (st[2] + cz) % nf[2] : 0;
       double wz = dim > 2 ? ker[2][cz] : 1.0;
@@ -436,14 +448,14 @@ void or_spread_es(int dim, int64_t M, const double *const *xyz, const double *sh
 /* c[j] = sum_g grid[g] phi(g - r_j) */
 void or_interp_es(int dim, int64_t M, const double *const *xyz, const double *shift,
                   const double *scale, const double *grid, const int *nf, int ns, double beta,
-                  double *c) {
+                  int ncoef, const double *coef, double *c) {
   const int n1 = dim > 1 ? ns : 1, n2 = dim > 2 ? ns : 1;
 #pragma omp parallel for schedule(static)
   for (int64_t j = 0; j < M; ++j) {
     double ker[3][32];
     int st[3] = {0, 0, 0};
     for (int d = 0; d < dim; ++d)
-      or_axis_es(xyz[d][j], shift[d], scale[d], nf[d], ns, beta, &st[d], ker[d]);
+      or_axis_es(xyz[d][j], shift[d], scale[d], nf[d], ns, beta, ncoef, coef, &st[d], ker[d]);
     double sr = 0, si = 0;
     for (int cz = 0; cz < n2; ++cz) {
       int64_t gz = dim > 2 ? (st[2] + cz) % nf[2] : 0;
@@ -464,175 +476,6 @@ void or_interp_es(int dim, int64_t M, const double *const *xyz, const double *sh
     c[2 * j + 1] = si;
   }
 }
-
-/* ------------------------- CPU-library-style spreader (OpenMP, Horner) ---- */
-/* The CPU library spreads bin-sorted points in subproblems: each thread fills
- * a private padded box, then adds it into the periodic fine grid
- * (include/finufft/spreadinterp.hpp:310-485, include/finufft/spread.hpp:53-451).
- * The kernel is given as ns pieces of ncoef Horner coefficients in
- * u = 2(x - piece start) - 1 (coef[k*ns + j], k = 0 highest degree); for the
- * CPU restatement they are fitted to the PSWF kernel by the Python side.
- * Arithmetic is in the plan precision T, as in the CPU library. */
-
-#define OR_MAXNS 16
-#define OR_DEFINE_CPU(T, SUF)                                                                \
-  /* fold (include/finufft/simd.hpp:318-325) and first cell / kernel argument */            \
-  static inline void or_place_##SUF(T x, int nf, int ns, int *i1, T *t0) {                  \
-    T r = (T)fma(x, (T)OR_INV_2PI, (T)0.5);                                                  \
-    r = (r - floor(r)) * (T)nf;                                                              \
-    T s = ceil(r - (T)0.5 * ns);                                                             \
-    *i1 = (int)s;                                                                            \
-    *t0 = s - r;                                                                             \
-  }                                                                                          \
-  static inline void or_horner_##SUF(const double *coef, int ns, int nc, T t0, T *ker) {    \
-    T u = (T)2 * t0 + (T)(ns - 1);                                                           \
-    for (int j = 0; j < ns; ++j) ker[j] = (T)coef[j];                                        \
-    for (int k = 1; k < nc; ++k)                                                             \
-      for (int j = 0; j < ns; ++j) ker[j] = ker[j] * u + (T)coef[k * ns + j];               \
-  }                                                                                          \
-  /* bin-sort permutation (CPU bins 16 x 4 x 4, stable) */                                  \
-  void or_cpu_sort_##SUF(int dim, int64_t M, const T *const *xyz, const int *nf,            \
-                         int32_t *perm) {                                                    \
-    const int bs[3] = {16, 4, 4};                                                            \
-    int nb[3] = {1, 1, 1};                                                                   \
-    for (int d = 0; d < dim; ++d) nb[d] = nf[d] / bs[d] + 1;                                 \
-    int64_t nbins = (int64_t)nb[0] * nb[1] * nb[2];                                          \
-    int64_t *cnt = (int64_t *)calloc((size_t)nbins + 1, sizeof(int64_t));                    \
-    uint32_t *key = (uint32_t *)malloc((size_t)(M > 0 ? M : 1) * sizeof(uint32_t));          \
-    _Pragma("omp parallel for schedule(static)") for (int64_t i = 0; i < M; ++i) {         \
-      int64_t k = 0, st = 1;                                                                 \
-      for (int d = 0; d < dim; ++d) {                                                        \
-        T r = (T)fma(xyz[d][i], (T)OR_INV_2PI, (T)0.5);                                      \
-        r = (r - floor(r)) * (T)nf[d];                                                       \
-        int b = (int)(r / bs[d]);                                                            \
-        if (b >= nb[d]) b = nb[d] - 1;                                                       \
-        if (b < 0) b = 0;                                                                    \
-        k += st * b;                                                                         \
-        st *= nb[d];                                                                         \
-      }                                                                                      \
-      key[i] = (uint32_t)k;                                                                  \
-    }                                                                                        \
-    for (int64_t i = 0; i < M; ++i) cnt[key[i] + 1]++;                                       \
-    for (int64_t b = 0; b < nbins; ++b) cnt[b + 1] += cnt[b];                                \
-    for (int64_t i = 0; i < M; ++i) perm[cnt[key[i]]++] = (int32_t)i;                        \
-    free(cnt);                                                                               \
-    free(key);                                                                               \
-  }                                                                                          \
-  /* grid (zeroed by caller) += spread of c over sorted points, subproblems of <= maxsub */ \
-  void or_cpu_spread_##SUF(int dim, int64_t M, const T *const *xyz, const int32_t *perm,    \
-                           const T *c, const int *nf, int ns, int nc, const double *coef,   \
-                           int maxsub, T *grid) {                                            \
-    const int64_t nsub = (M + maxsub - 1) / maxsub;                                          \
-    const int64_t n0 = nf[0], n1 = dim > 1 ? nf[1] : 1, n2 = dim > 2 ? nf[2] : 1;           \
-    _Pragma("omp parallel for schedule(dynamic, 1)") for (int64_t sp = 0; sp < nsub; ++sp) { \
-      const int64_t p0 = sp * maxsub, p1 = p0 + maxsub < M ? p0 + maxsub : M;                \
-      int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-(1 << 30), -(1 << 30), -(1 << 30)}; \
-      for (int64_t p = p0; p < p1; ++p)                                                      \
-        for (int d = 0; d < dim; ++d) {                                                      \
-          int i1;                                                                            \
-          T t0;                                                                              \
-          or_place_##SUF(xyz[d][perm[p]], nf[d], ns, &i1, &t0);                              \
-          if (i1 < lo[d]) lo[d] = i1;                                                        \
-          if (i1 > hi[d]) hi[d] = i1;                                                        \
-        }                                                                                    \
-      int64_t ext[3] = {1, 1, 1};                                                            \
-      for (int d = 0; d < dim; ++d) ext[d] = hi[d] - lo[d] + ns;                             \
-      T *box = (T *)calloc((size_t)(2 * ext[0] * ext[1] * ext[2]), sizeof(T));               \
-      T kx[OR_MAXNS], ky[OR_MAXNS], kz[OR_MAXNS];                                            \
-      for (int64_t p = p0; p < p1; ++p) {                                                    \
-        const int64_t j = perm[p];                                                           \
-        int ix, iy = 0, iz = 0;                                                              \
-        T t0;                                                                                \
-        or_place_##SUF(xyz[0][j], nf[0], ns, &ix, &t0);                                      \
-        or_horner_##SUF(coef, ns, nc, t0, kx);                                               \
-        if (dim > 1) {                                                                       \
-          or_place_##SUF(xyz[1][j], nf[1], ns, &iy, &t0);                                    \
-          or_horner_##SUF(coef, ns, nc, t0, ky);                                             \
-        } else                                                                               \
-          ky[0] = 1;                                                                         \
-        if (dim > 2) {                                                                       \
-          or_place_##SUF(xyz[2][j], nf[2], ns, &iz, &t0);                                    \
-          or_horner_##SUF(coef, ns, nc, t0, kz);                                             \
-        } else                                                                               \
-          kz[0] = 1;                                                                         \
-        const T cr = c[2 * j], ci = c[2 * j + 1];                                            \
-        const int ny = dim > 1 ? ns : 1, nz = dim > 2 ? ns : 1;                              \
-        for (int a = 0; a < nz; ++a)                                                         \
-          for (int b = 0; b < ny; ++b) {                                                     \
-            const T w = ky[b] * kz[a];                                                       \
-            const T wr = cr * w, wi = ci * w;                                                \
-            T *row = box + 2 * ((ix - lo[0]) +                                               \
-                                ext[0] * ((dim > 1 ? iy - lo[1] + b : 0) +                   \
-                                          ext[1] * (dim > 2 ? iz - lo[2] + a : 0)));         \
-            for (int q = 0; q < ns; ++q) {                                                   \
-              row[2 * q] += wr * kx[q];                                                      \
-              row[2 * q + 1] += wi * kx[q];                                                  \
-            }                                                                                \
-          }                                                                                  \
-      }                                                                                      \
-      for (int64_t bz = 0; bz < ext[2]; ++bz) {                                              \
-        int64_t gz = dim > 2 ? ((lo[2] + bz) % n2 + n2) % n2 : 0;                            \
-        for (int64_t by = 0; by < ext[1]; ++by) {                                            \
-          int64_t gy = dim > 1 ? ((lo[1] + by) % n1 + n1) % n1 : 0;                          \
-          const T *row = box + 2 * ext[0] * (by + ext[1] * bz);                              \
-          for (int64_t bx = 0; bx < ext[0]; ++bx) {                                          \
-            int64_t gx = ((lo[0] + bx) % n0 + n0) % n0;                                      \
-            T *g = grid + 2 * (gx + n0 * (gy + n1 * gz));                                    \
-            _Pragma("omp atomic") g[0] += row[2 * bx];                                       \
-            _Pragma("omp atomic") g[1] += row[2 * bx + 1];                                   \
-          }                                                                                  \
-        }                                                                                    \
-      }                                                                                      \
-      free(box);                                                                             \
-    }                                                                                        \
-  }                                                                                          \
-  /* c[j] = interpolation of the periodic grid at the points (sorted traversal) */          \
-  void or_cpu_interp_##SUF(int dim, int64_t M, const T *const *xyz, const int32_t *perm,    \
-                           const T *grid, const int *nf, int ns, int nc, const double *coef, \
-                           T *c) {                                                           \
-    const int64_t n0 = nf[0], n1 = dim > 1 ? nf[1] : 1, n2 = dim > 2 ? nf[2] : 1;           \
-    _Pragma("omp parallel for schedule(static, 4096)") for (int64_t p = 0; p < M; ++p) {    \
-      const int64_t j = perm[p];                                                             \
-      T kx[OR_MAXNS], ky[OR_MAXNS], kz[OR_MAXNS];                                            \
-      int ix, iy = 0, iz = 0;                                                                \
-      T t0;                                                                                  \
-      or_place_##SUF(xyz[0][j], nf[0], ns, &ix, &t0);                                        \
-      or_horner_##SUF(coef, ns, nc, t0, kx);                                                 \
-      if (dim > 1) {                                                                         \
-        or_place_##SUF(xyz[1][j], nf[1], ns, &iy, &t0);                                      \
-        or_horner_##SUF(coef, ns, nc, t0, ky);                                               \
-      } else                                                                                 \
-        ky[0] = 1;                                                                           \
-      if (dim > 2) {                                                                         \
-        or_place_##SUF(xyz[2][j], nf[2], ns, &iz, &t0);                                      \
-        or_horner_##SUF(coef, ns, nc, t0, kz);                                               \
-      } else                                                                                 \
-        kz[0] = 1;                                                                           \
-      T sr = 0, si = 0;                                                                      \
-      const int ny = dim > 1 ? ns : 1, nz = dim > 2 ? ns : 1;                                \
-      for (int a = 0; a < nz; ++a) {                                                         \
-        int64_t gz = dim > 2 ? ((iz + a) % n2 + n2) % n2 : 0;                                \
-        for (int b = 0; b < ny; ++b) {                                                       \
-          int64_t gy = dim > 1 ? ((iy + b) % n1 + n1) % n1 : 0;                              \
-          const T w = ky[b] * kz[a];                                                         \
-          T rr = 0, ri = 0;                                                                  \
-          for (int q = 0; q < ns; ++q) {                                                     \
-            int64_t gx = ((ix + q) % n0 + n0) % n0;                                          \
-            const T *g = grid + 2 * (gx + n0 * (gy + n1 * gz));                              \
-            rr += kx[q] * g[0];                                                              \
-            ri += kx[q] * g[1];                                                              \
-          }                                                                                  \
-          sr += w * rr;                                                                      \
-          si += w * ri;                                                                      \
-        }                                                                                    \
-      }                                                                                      \
-      c[2 * j] = sr;                                                                         \
-      c[2 * j + 1] = si;                                                                     \
-    }                                                                                        \
-  }
-
-OR_DEFINE_CPU(float, f)
-OR_DEFINE_CPU(double, d)
 
 int or_num_threads(void) {
 #ifdef _OPENMP

@@ -54,8 +54,8 @@ def lib():
         L.or_dirft1.argtypes = [i, I64, P, P, i, P, I64, P, P]
         L.or_dirft2.argtypes = [i, I64, P, i, P, P, I64, P, P]
         L.or_dirft3.argtypes = [i, I64, P, P, i, P, I64, P, P]
-        L.or_spread_es.argtypes = [i, I64, P, P, P, P, P, i, d, P]
-        L.or_interp_es.argtypes = [i, I64, P, P, P, P, P, i, d, P]
+        L.or_spread_es.argtypes = [i, I64, P, P, P, P, P, i, d, i, P, P]
+        L.or_interp_es.argtypes = [i, I64, P, P, P, P, P, i, d, i, P, P]
         for suf in ("f", "d"):
             getattr(L, "or_cpu_sort_" + suf).argtypes = [i, I64, P, P, P]
             getattr(L, "or_cpu_spread_" + suf).argtypes = [i, I64, P, P, P, P, i, i, P, i, P]
@@ -164,6 +164,23 @@ def cpu_kernel(tol, dim, nufft_type, sigma=2.0, is_float=False, clip=True):
             ns = min(ns, 8)
     beta = PI * ns * (1 - 1 / (2 * sigma)) - 0.05
     return ns, beta
+
+
+def engine_kernel(tol, sigma=2.0, dim=3, nufft_type=1, is_float=True, kernel="pswf"):
+    """The engine's kernel choice: (ns, beta, phi, horner table or None).
+
+    kernel "es": the GPU library's rule and ES kernel (src/cuda/makeplan.cu:43-119);
+    "pswf": the CPU library's PSWF (src/common/kernel.cpp:79-146, kerformula 8)
+    with width max(CPU width law, GPU rule), clipped to 12 (float) / 16."""
+    ns_g, beta_g = gpu_kernel(tol, sigma, 0 if sigma not in (2.0, 1.25) else 1, is_float)
+    if kernel == "es":
+        return ns_g, beta_g, (lambda x: es_kernel(x, ns_g, beta_g)), None
+    eps = max(tol, np.finfo(np.float32 if is_float else np.float64).eps)
+    ns_c = cpu_kernel(eps, dim, nufft_type, sigma, is_float, clip=False)[0]
+    ns = max(2, min(max(ns_c, ns_g), 12 if is_float else 16))
+    beta = PI * ns * (1 - 1 / (2 * sigma)) - 0.05
+    fun = lambda x: pswf0(beta, 2.0 * np.asarray(x) / ns)
+    return ns, beta, fun, np.ascontiguousarray(horner_table(fun, ns, min(ns + 6, 24)))
 
 
 def horner_table(fun, ns, ncoef):
@@ -287,7 +304,7 @@ def _phihat_series(fun, ns, nf):
     return ph * np.where(k % 2 == 1, -1.0, 1.0)
 
 
-def _spread(xs, c, nf, ns, beta, shift=None, scale=None):
+def _spread(xs, c, nf, ns, beta, shift=None, scale=None, coef=None):
     dim = len(xs)
     xs = _coords(xs)
     c = _cplx(c)
@@ -295,12 +312,13 @@ def _spread(xs, c, nf, ns, beta, shift=None, scale=None):
     sc = np.ones(3) if scale is None else np.asarray(list(scale) + [1] * (3 - dim), np.float64)
     nfa = np.array(list(nf) + [1] * (3 - dim), dtype=np.int32)
     grid = np.zeros(int(np.prod(nfa)), dtype=np.complex128)
+    nco = 0 if coef is None else coef.shape[0]
     lib().or_spread_es(dim, len(xs[0]), _ptrs(xs), _ptr(sh), _ptr(sc), _ptr(c), _ptr(nfa), ns,
-                       beta, _ptr(grid))
+                       beta, nco, _ptr(coef), _ptr(grid))
     return grid.reshape(tuple(reversed(list(nf))))
 
 
-def _interp(xs, grid, nf, ns, beta, shift=None, scale=None):
+def _interp(xs, grid, nf, ns, beta, shift=None, scale=None, coef=None):
     dim = len(xs)
     xs = _coords(xs)
     g = _cplx(grid).reshape(-1)
@@ -308,8 +326,9 @@ def _interp(xs, grid, nf, ns, beta, shift=None, scale=None):
     sc = np.ones(3) if scale is None else np.asarray(list(scale) + [1] * (3 - dim), np.float64)
     nfa = np.array(list(nf) + [1] * (3 - dim), dtype=np.int32)
     out = np.zeros(len(xs[0]), dtype=np.complex128)
+    nco = 0 if coef is None else coef.shape[0]
     lib().or_interp_es(dim, len(xs[0]), _ptrs(xs), _ptr(sh), _ptr(sc), _ptr(g), _ptr(nfa), ns,
-                       beta, _ptr(out))
+                       beta, nco, _ptr(coef), _ptr(out))
     return out
 
 
@@ -341,8 +360,9 @@ def _grid_take(grid, n_modes, nf, modeord):
 
 
 def nufft_es(nufft_type, xs, data, isign, tol, n_modes=None, ss=None, sigma=None,
-             is_float=True, modeord=0):
-    """The GPU library's algorithm with its ES kernel, entirely in FP64.
+             is_float=True, modeord=0, kernel="es"):
+    """The GPU library's algorithm, entirely in FP64, with its ES kernel
+    (kernel="es") or with the engine's default PSWF kernel (kernel="pswf").
 
     Types 1/2: n_modes (x fastest); data is c[M] (type 1) or f with shape
     reversed(n_modes) (type 2). Type 3: ss = target coordinates."""
@@ -352,14 +372,18 @@ def nufft_es(nufft_type, xs, data, isign, tol, n_modes=None, ss=None, sigma=None
         # precision only at tol >= 1e-4 (compared in single precision)
         ok = np.float32(tol) >= np.float32(1e-4) if is_float else tol >= 1e-9
         sigma = 1.25 if (nufft_type == 3 and tol >= 1e-9 and ok) else 2.0
-    ns, beta = gpu_kernel(tol, sigma, 1, is_float)
-    fun = lambda x: es_kernel(x, ns, beta)
+    ns, beta, fun, coef = engine_kernel(tol, sigma, dim, nufft_type, is_float, kernel)
+    if nufft_type == 3 and kernel == "pswf":
+        # the inner type-2 plan chooses its own (type-2) width
+        ns2, beta2, fun2, coef2 = engine_kernel(tol, sigma, dim, 2, is_float, kernel)
+    else:
+        ns2, beta2, fun2, coef2 = ns, beta, fun, coef
     if nufft_type in (1, 2):
         nf = [fine_grid(m, sigma, ns) for m in n_modes]
         ph = [_phihat_series(fun, ns, n) for n in nf]
         axes = tuple(range(dim))
         if nufft_type == 1:
-            G = _fft_sign(_spread(xs, data, nf, ns, beta), isign, axes)
+            G = _fft_sign(_spread(xs, data, nf, ns, beta, coef=coef), isign, axes)
             return _grid_take(G, n_modes, nf, modeord) * _deconv_factor(n_modes, nf, ph, modeord)
         fk = np.asarray(data, dtype=np.complex128).reshape(tuple(reversed(list(n_modes))))
         grid = np.zeros(tuple(reversed(nf)), dtype=np.complex128)
@@ -368,7 +392,7 @@ def nufft_es(nufft_type, xs, data, isign, tol, n_modes=None, ss=None, sigma=None
             k = _mode_index(n_modes[d], modeord)
             idx.append(np.where(k >= 0, k, nf[d] + k))
         grid[np.ix_(*idx)] = fk * _deconv_factor(n_modes, nf, ph, modeord)
-        return _interp(xs, _fft_sign(grid, isign, axes), nf, ns, beta)
+        return _interp(xs, _fft_sign(grid, isign, axes), nf, ns, beta, coef=coef)
     # type 3
     xs, ss = _coords(xs), _coords(ss)
     X, C, S, D = [], [], [], []
@@ -382,18 +406,19 @@ def nufft_es(nufft_type, xs, data, isign, tol, n_modes=None, ss=None, sigma=None
         a, b, g = type3_grid(sigma, X[d], S[d], ns)
         nf.append(a), h.append(b), gam.append(g)
     pre = np.exp(1j * isign * sum(D[d] * xs[d] for d in range(dim)))
-    grid = _spread(xs, np.asarray(data) * pre, nf, ns, beta, shift=C, scale=[1 / g for g in gam])
+    grid = _spread(xs, np.asarray(data) * pre, nf, ns, beta, shift=C, scale=[1 / g for g in gam],
+                   coef=coef)
     # inner type 2 on the grid (mode m at position m + nf/2) at s' = h gam (s - D)
     sp = [h[d] * gam[d] * (ss[d] - D[d]) for d in range(dim)]
-    nf2 = [fine_grid(n, sigma, ns) for n in nf]
-    ph2 = [_phihat_series(fun, ns, n) for n in nf2]
+    nf2 = [fine_grid(n, sigma, ns2) for n in nf]
+    ph2 = [_phihat_series(fun2, ns2, n) for n in nf2]
     g2 = np.zeros(tuple(reversed(nf2)), dtype=np.complex128)
     idx = []
     for d in reversed(range(dim)):
         k = _mode_index(nf[d], 0)
         idx.append(np.where(k >= 0, k, nf2[d] + k))
     g2[np.ix_(*idx)] = grid * _deconv_factor(nf, nf2, ph2, 0)
-    vals = _interp(sp, _fft_sign(g2, isign, tuple(range(dim))), nf2, ns, beta)
+    vals = _interp(sp, _fft_sign(g2, isign, tuple(range(dim))), nf2, ns2, beta2, coef=coef2)
     phis = np.ones(len(ss[0]))
     for d in range(dim):
         phis = phis * kernel_ft(fun, ns, sp[d], 2.0)
@@ -405,7 +430,13 @@ def nufft_es(nufft_type, xs, data, isign, tol, n_modes=None, ss=None, sigma=None
 class CpuPlan:
     """The CPU library's pipeline with its PSWF kernel (sigma fixed, default 2):
     bin sort at setpts, then spread (OpenMP C) -> FFT (scipy, all threads) ->
-    deconvolve, or the reverse for type 2. Precision follows dtype."""
+    deconvolve, or the reverse for type 2. Precision follows dtype.
+    Type 3 (n_modes = the dimension): see CpuPlan3."""
+
+    def __new__(cls, nufft_type, *args, **kw):
+        if nufft_type == 3 and cls is CpuPlan:
+            return CpuPlan3(*args, **kw)
+        return super().__new__(cls)
 
     def __init__(self, nufft_type, n_modes, isign, tol, dtype=np.complex64, sigma=2.0,
                  threads=None, maxsub=10000):
@@ -469,3 +500,70 @@ class CpuPlan:
             self.dim, self.M, self._px, _ptr(self.perm), _ptr(G), _ptr(self._nfa), self.ns,
             self.ncoef, _ptr(self.coef), _ptr(out))
         return out
+
+
+class CpuPlan3:
+    """The CPU library's type 3 (include/finufft/setpts.hpp:163-319 and
+    execute.hpp type-3 branch) with its PSWF kernel: sources rescaled to
+    x' = (x - C)/gamma, pre-phase exp(i isign D.x), spread onto the outer grid
+    of nhg_type3 (type-3 kernel width), an inner type-2 CpuPlan at the same tol
+    on that grid evaluated at s' = h gamma (s - D), and the post factor
+    exp(i isign (s - D).C) / prod phihat(s'). sigma is fixed (default 2; the
+    CPU library picks it by a cost model at setpts)."""
+
+    def __init__(self, dim, isign, tol, dtype=np.complex64, sigma=2.0, threads=None,
+                 maxsub=10000):
+        self.dim, self.isign, self.tol, self.sigma = int(dim), isign, tol, sigma
+        self.is_float = np.dtype(dtype) == np.complex64
+        self.cdt = np.complex64 if self.is_float else np.complex128
+        self.rdt = np.float32 if self.is_float else np.float64
+        self.ns, self.beta = cpu_kernel(tol, self.dim, 3, sigma, self.is_float)
+        self.fun = lambda x: pswf0(self.beta, 2.0 * np.asarray(x) / self.ns)
+        self.ncoef = self.ns + 4
+        self.coef = np.ascontiguousarray(horner_table(self.fun, self.ns, self.ncoef))
+        self.threads = threads or lib().or_num_threads()
+        self.maxsub = maxsub
+        self.dtype = dtype
+
+    def setpts(self, xs, ss):
+        dim = self.dim
+        xs = [np.asarray(a, dtype=np.float64) for a in xs]
+        ss = [np.asarray(a, dtype=np.float64) for a in ss]
+        self.M, self.N = len(xs[0]), len(ss[0])
+        X, C, S, D = [], [], [], []
+        for d in range(dim):
+            w, c0 = width_center(xs[d].min(), xs[d].max()) if self.M else (0.0, 0.0)
+            X.append(w), C.append(c0)
+            w, c0 = width_center(ss[d].min(), ss[d].max()) if self.N else (0.0, 0.0)
+            S.append(w), D.append(c0)
+        self.nf, h, gam = [], [], []
+        for d in range(dim):
+            a, b, g = type3_grid(self.sigma, X[d], S[d], self.ns)
+            self.nf.append(a), h.append(b), gam.append(g)
+        self.xp = [np.ascontiguousarray((xs[d] - C[d]) / gam[d], dtype=self.rdt)
+                   for d in range(dim)]
+        self.pre = np.exp(1j * self.isign * sum(D[d] * xs[d] for d in range(dim))).astype(self.cdt)
+        sp = [h[d] * gam[d] * (ss[d] - D[d]) for d in range(dim)]
+        phis = np.ones(self.N)
+        for d in range(dim):
+            phis = phis * kernel_ft(self.fun, self.ns, sp[d], 2.0)
+        self.post = (np.exp(1j * self.isign * sum(C[d] * (ss[d] - D[d]) for d in range(dim)))
+                     / phis).astype(self.cdt)
+        self.perm = np.zeros(max(self.M, 1), dtype=np.int32)
+        self._nfa = np.array(self.nf + [1] * (3 - dim), dtype=np.int32)
+        self._px = _ptrs(self.xp)
+        suf = "f" if self.is_float else "d"
+        getattr(lib(), "or_cpu_sort_" + suf)(dim, self.M, self._px, _ptr(self._nfa),
+                                             _ptr(self.perm))
+        self.inner = CpuPlan(2, self.nf, self.isign, self.tol, dtype=self.dtype,
+                             sigma=self.sigma, threads=self.threads, maxsub=self.maxsub)
+        self.inner.setpts([np.ascontiguousarray(a, dtype=self.rdt) for a in sp])
+
+    def execute(self, c):
+        suf = "f" if self.is_float else "d"
+        cp = np.ascontiguousarray(np.asarray(c, dtype=self.cdt) * self.pre)
+        grid = np.zeros(tuple(reversed(self.nf)), dtype=self.cdt)
+        getattr(lib(), "or_cpu_spread_" + suf)(
+            self.dim, self.M, self._px, _ptr(self.perm), _ptr(cp), _ptr(self._nfa), self.ns,
+            self.ncoef, _ptr(self.coef), self.maxsub, _ptr(grid))
+        return self.inner.execute(grid) * self.post

@@ -191,12 +191,21 @@ def test_host_pointer_api(oracle, engine, prec):
     f = np.zeros(nm[0] * nm[1], dtype=cdt)
     assert getattr(engine, pfx + "_execute")(p, c.ctypes.data, f.ctypes.data) == 0
     ref = oracle.dirft1([x, y], c, 1, nm)
-    assert oracle.rel_l2(f, ref) < 20 * tol
+    # the accuracy contract: no worse than twice the CPU library's error at the
+    # same tol (its algorithm restated in the oracle, same precision and inputs)
+    cpu = oracle.CpuPlan(1, list(nm), 1, tol, dtype=cdt)
+    cpu.setpts([x, y])
+    cpu_err = oracle.rel_l2(cpu.execute(c).ravel(), ref)
+    assert oracle.rel_l2(f, ref) < 2 * cpu_err
     # adjoint of type 1 = type 2 with the opposite sign, modes -> points
     g = _cx(rng, nm[0] * nm[1], cdt)
     cc = np.zeros(M, dtype=cdt)
     assert getattr(engine, pfx + "_execute_adjoint")(p, cc.ctypes.data, g.ctypes.data) == 0
-    assert oracle.rel_l2(cc, oracle.dirft2([x, y], g, -1, nm)) < 20 * tol
+    ref2 = oracle.dirft2([x, y], g, -1, nm)
+    cpu2 = oracle.CpuPlan(2, list(nm), -1, tol, dtype=cdt)
+    cpu2.setpts([x, y])
+    cpu2_err = oracle.rel_l2(cpu2.execute(g), ref2)
+    assert oracle.rel_l2(cc, ref2) < 2 * cpu2_err
     assert getattr(engine, pfx + "_destroy")(p) == 0
 
 
@@ -225,6 +234,19 @@ def test_host_pointer_pipelined_batches(oracle, engine, ty):
     assert engine.finufftf_setpts(p, M, x.ctypes.data, y.ctypes.data, z.ctypes.data,
                                   K if ty == 3 else 0, ptr(s), ptr(t), ptr(u)) == 0
     nout = K if ty == 3 else int(np.prod(nm))
+    # bar: the same algorithm in FP64 (the plan's PSWF kernel) plus float rounding
+    xo = [x.astype(np.float64), y.astype(np.float64), z.astype(np.float64)]
+
+    def bar(k_in, ref):
+        if ty == 1:
+            same = oracle.nufft_es(1, xo, k_in, 1, tol, n_modes=nm, kernel="pswf").ravel()
+        elif ty == 2:
+            same = oracle.nufft_es(2, xo, k_in.reshape(nm[::-1]), -1, tol, n_modes=nm,
+                                   kernel="pswf")
+        else:
+            same = oracle.nufft_es(3, xo, k_in, 1, tol, ss=[s, t, u], kernel="pswf")
+        return 1.25 * oracle.rel_l2(same, ref) + 5e-6
+
     for pinned in (True, False):
         if ty == 2:
             fin = _cx(rng, (ntr, int(np.prod(nm))))
@@ -234,7 +256,7 @@ def test_host_pointer_pipelined_batches(oracle, engine, ty):
             assert engine.finufftf_execute(p, cout.ctypes.data, fh.numpy().ctypes.data) == 0
             for k in range(ntr):
                 ref = oracle.dirft2([x, y, z], fin[k], -1, nm)
-                assert oracle.rel_l2(cout[k * M:(k + 1) * M], ref) < 20 * tol
+                assert oracle.rel_l2(cout[k * M:(k + 1) * M], ref) < bar(fin[k], ref)
         else:
             cin = _cx(rng, (ntr, M))
             ch = torch.from_numpy(cin.ravel().copy())
@@ -246,7 +268,7 @@ def test_host_pointer_pipelined_batches(oracle, engine, ty):
                     ref = oracle.dirft1([x, y, z], cin[k], 1, nm)
                 else:
                     ref = oracle.dirft3([x, y, z], cin[k], 1, [s, t, u])
-                assert oracle.rel_l2(fout[k * nout:(k + 1) * nout], ref) < 20 * tol
+                assert oracle.rel_l2(fout[k * nout:(k + 1) * nout], ref) < bar(cin[k], ref)
     assert engine.finufftf_destroy(p) == 0
 
 

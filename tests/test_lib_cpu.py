@@ -94,3 +94,54 @@ def test_host_api_host_side_errors(engine, pfx):
     assert _mk(engine, pfx, 1, 1, (10, 1, 1), ntr=0) == 9  # FINUFFT_ERR_NTRANS_NOTVALID
     assert _mk(engine, pfx, 1, 1, (10, 1, 1), tol=1e-30) == 26  # FINUFFT_ERR_EPS_TOO_SMALL
     assert getattr(engine, pfx + "_destroy")(None) == 16
+
+
+def test_pswf_kernel_values_against_reference(engine):
+    """the engine's PSWF (the CPU library's kernel, which the default plans fit
+    their Horner pieces to) equals the reference's own psi_0 (src/common/pswf.cpp,
+    golden values generated from the reference tree) to rounding"""
+    import json
+
+    import numpy as np
+
+    g = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_planning.json")))
+    z = np.array(g["pswf"]["z"])
+    for c, vals in g["pswf"]["values"].items():
+        ns = 8
+        x = np.ascontiguousarray(z * ns / 2)
+        out = np.zeros_like(x)
+        assert engine.gbnufft_kernel_eval(2, ns, float(c), len(x), x.ctypes.data,
+                                          out.ctypes.data) == 0
+        assert np.abs(out - np.array(vals)).max() < 2e-15, c
+
+
+def test_kernel_choice_rules(engine, oracle):
+    """width/shape rules: the ES form is the GPU library's (src/cuda/makeplan.cu:
+    43-119), the PSWF form the CPU library's (src/common/kernel.cpp:79-146,
+    golden values from the reference) widened to the GPU rule where that is
+    wider, as the oracle's engine_kernel states it"""
+    import json
+
+    g = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_planning.json")))
+    ns, beta = ctypes.c_int(), ctypes.c_double()
+    for tol, dim, ty, sigma, ref_ns, ref_beta in g["cpu_kernel"]:
+        for f32 in (0, 1):
+            assert engine.gbnufft_kernel_choice(tol, sigma, dim, ty, f32, 2, 0, ctypes.byref(ns),
+                                                ctypes.byref(beta)) == 0
+            want = oracle.engine_kernel(tol, sigma, dim, ty, bool(f32), "pswf")
+            assert (ns.value, beta.value) == (want[0], pytest.approx(want[1], rel=1e-14))
+            gpu_ns = oracle.gpu_kernel(max(tol, 1.2e-7 if f32 else 2.3e-16), sigma, 0, bool(f32))[0]
+            if ref_ns <= (12 if f32 else 16) and tol >= (1.2e-7 if f32 else 2.3e-16):
+                assert ns.value == max(ref_ns, gpu_ns)
+                if ns.value == ref_ns:
+                    assert beta.value == pytest.approx(ref_beta, rel=1e-14)
+        assert engine.gbnufft_kernel_choice(tol, sigma, dim, ty, 0, 1, 0, ctypes.byref(ns),
+                                            ctypes.byref(beta)) == 0
+        want = oracle.gpu_kernel(tol, sigma, 0, False)
+        assert (ns.value, beta.value) == (want[0], pytest.approx(want[1], rel=1e-12))
+    # kerformula: 7, 8, 9 are PSWF shape choices; 1-6 (the removed kernels) are errors
+    for kf in (7, 8, 9):
+        assert engine.gbnufft_kernel_choice(1e-6, 2.0, 2, 1, 0, 2, kf, ctypes.byref(ns),
+                                            ctypes.byref(beta)) == 0
+    assert engine.gbnufft_kernel_choice(1e-6, 2.0, 2, 1, 0, 2, 3, ctypes.byref(ns),
+                                        ctypes.byref(beta)) == 24  # KERFORMULA_NOTVALID
