@@ -8,16 +8,30 @@ Synthetic, seeded inputs of those shapes stand in for user data.
 A step is one execute of the planned transform on resident device inputs
 (spread -> FFT -> deconvolve), timed with CUDA events on the plan's stream.
 ``value`` is the planned+batched form (ntransf strength vectors sharing the
-points, one CUDA-graph replay per step); the plain form (one transform,
-default options) is reported beside it. ``e2e`` times the same batched
-transform through the public API with host buffers: pinned H2D of the step's
-strengths, execute, D2H of the modes. Inputs (800 MB of strengths per vector,
-a 1 GB fine grid per vector) exceed the 129 MB L2, so no flush is needed.
+points, one CUDA-graph replay per step). Beside it:
+  * ``plain``: one transform planned by the reference library's heuristic
+    (planner 1: its bin sizes, method, subproblem size and ES kernel), no
+    batching, no graph -- the plain GPU form;
+  * ``plain_engine``: one transform with this engine's own planning;
+  * ``e2e``: the batched transform through the host-pointer C ABI
+    (finufftf_execute) with pinned host buffers, copies inside the timed region;
+  * ``accuracy``: relative l2 error on 1e3 sampled modes (a seeded 10x10x10
+    grid of mode indices) against an FP64 direct sum, for the engine and for
+    the CPU restatement of FINUFFT on the same inputs at the same tol;
+  * ``cpu_baseline``: that CPU restatement (OpenMP, all host cores) timed on
+    one execute of one strength vector over all 1e8 points;
+  * ``configs``: the other workloads (C1 1D FP64, C2 2D type 2 x16, C4 4096
+    uneven 2D problems, C5 3D type 3, C3 in FP64 at tol 1e-12), each with its
+    throughput, its error on sampled outputs against FP64 direct sums, the CPU
+    restatement's error on the same inputs and the ratio of the two.
+Inputs (800 MB of strengths per vector, a 1 GB fine grid per vector) exceed
+the 129 MB L2, so no flush is needed.
 
---impl reference times the CPU restatement of FINUFFT's algorithm (the
-oracle port, PSWF kernel, OpenMP spreading + threaded FFT) on the host cores.
-Under torchrun each rank runs an independent replica (the transform does not
-shard); value sums the replicas.
+--impl reference times the CPU restatement of FINUFFT's algorithm (the oracle
+port, PSWF kernel, OpenMP spreading + threaded FFT) on the host cores: each
+step is one execute of one strength vector over all 1e8 points. Under torchrun
+each rank runs an independent replica (the transform does not shard); value
+sums the replicas.
 """
 import argparse
 import json
@@ -36,6 +50,8 @@ N_MODES = (256, 256, 256)
 M_FULL = 100_000_000
 TOL = 1e-5
 METRIC = "3D type-1 NU pts/s @tol 1e-5: planned+batched vs plain GPU vs CPU FINUFFT"
+WORKLOAD = ("3D type 1, 256^3 modes, M=1e8 clustered (8 Gaussians sigma 0.3 + 20% uniform), "
+            "complex64, tol 1e-5, iflag +1")
 
 
 def clustered_points(M, seed, rng_dev="cpu"):
@@ -56,11 +72,13 @@ def clustered_points(M, seed, rng_dev="cpu"):
     return pts
 
 
-def strengths(n, M, seed, dev):
+def strengths(n, M, seed, dev, dtype=None):
     import torch
 
+    dtype = dtype or torch.float32
     g = torch.Generator(device=dev).manual_seed(seed)
-    return torch.randn(n, M, 2, generator=g, device=dev, dtype=torch.float32).view(torch.complex64)[..., 0]
+    z = torch.randn(n, M, 2, generator=g, device=dev, dtype=dtype)
+    return z.view(torch.complex64 if dtype == torch.float32 else torch.complex128)[..., 0]
 
 
 class ClockSampler:
@@ -144,6 +162,105 @@ def time_steps(fn, stream, steps, warmup):
     return a.elapsed_time(b) / steps  # ms per step
 
 
+def measured_peak(key):
+    """a peak from MEASURED_PEAKS.json at the repository root (None if absent)"""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)[key])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+# DRAM bytes (read + write) per point per transform of the default 3D spread
+# kernel (int32 fixed-point tile), from the ncu capture at the same point
+# density (1.25e7 clustered points on a 256^3 grid: 987 MB read + 141 MB
+# written); scaled by points and transforms to one launch of this workload
+SPREAD_DRAM_BYTES_PER_POINT = (987e6 + 141e6) / 12.5e6
+
+
+# ------------------------------------------------------------------ accuracy ----
+def sample_axes(n_modes, per_axis, seed):
+    """seeded mode indices per array axis (row-major): their product grid is the
+    sample (per_axis ** dim modes)"""
+    g = np.random.default_rng(seed)
+    return [np.sort(g.choice(n, size=min(per_axis, n), replace=False)) for n in n_modes]
+
+
+def direct_type1_grid(coords, c, n_modes, axes_idx, isign, dev, chunk=1 << 20):
+    """FP64 direct type-1 sums f[k] = sum_j c_j exp(i isign k.x_j) on the
+    product grid of the given per-axis mode indices (modes k = idx - n//2;
+    coords[a] pairs with array axis a), on the GPU: the exponential separates
+    over axes, so each chunk of points is one complex GEMM."""
+    import torch
+
+    dim = len(n_modes)
+    ks = [torch.tensor(idx - n // 2, dtype=torch.float64, device=dev)
+          for idx, n in zip(axes_idx, n_modes)]
+    L = [len(k) for k in ks]
+    out = torch.zeros(int(np.prod(L)), dtype=torch.complex128, device=dev)
+    M = coords[0].numel()
+    for j0 in range(0, M, chunk):
+        j1 = min(M, j0 + chunk)
+        E = [torch.polar(torch.ones(1, dtype=torch.float64, device=dev),
+                         isign * ks[a][:, None] * coords[a][j0:j1].to(torch.float64)[None, :])
+             for a in range(dim)]
+        w = c[j0:j1].to(torch.complex128)
+        if dim == 1:
+            out += E[0] @ w
+        elif dim == 2:
+            out += (E[0] @ (E[1] * w[None, :]).T).reshape(-1)
+        else:
+            P = (E[1][:, None, :] * (E[2] * w[None, :])[None, :, :]).reshape(L[1] * L[2], -1)
+            out += (E[0] @ P.T).reshape(-1)
+    return out.reshape(L)
+
+
+def take_grid(f, axes_idx):
+    """f restricted to the product grid of per-axis indices"""
+    import torch
+
+    if isinstance(f, np.ndarray):
+        return f[np.ix_(*axes_idx)]
+    idx = [torch.as_tensor(a, device=f.device) for a in axes_idx]
+    for a, ix in enumerate(idx):
+        f = f.index_select(a, ix)
+    return f
+
+
+def rel_l2(a, b):
+    import torch
+
+    a = torch.as_tensor(a).to(torch.complex128).reshape(-1).cpu()
+    b = torch.as_tensor(b).to(torch.complex128).reshape(-1).cpu()
+    return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+
+
+def acc_entry(gpu_err, cpu_err, sample):
+    return {"gpu_rel_l2": gpu_err, "cpu_rel_l2": cpu_err,
+            "ratio_gpu_over_cpu": (gpu_err / cpu_err) if cpu_err else None, "sample": sample}
+
+
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    return O
+
+
+def cpu_type1_3d(pts_np, c_np, tol, dtype):
+    """CPU restatement (oracle port of FINUFFT's CPU algorithm, PSWF kernel,
+    OpenMP) of the metric transform: (modes array, setpts s, execute s, threads)."""
+    O = _oracle()
+    plan = O.CpuPlan(1, list(N_MODES[::-1]), +1, tol, dtype=dtype)
+    t0 = time.perf_counter()
+    plan.setpts([pts_np[2], pts_np[1], pts_np[0]])  # fastest axis first
+    t1 = time.perf_counter()
+    f = plan.execute(c_np)
+    t2 = time.perf_counter()
+    return f, t1 - t0, t2 - t1, plan.threads
+
+
+# --------------------------------------------------------------- metric (C3) ----
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -174,29 +291,40 @@ def run_gpu(args):
     nt = args.ntransf
     c = strengths(nt, M, 99 + rank, dev)
     stream = torch.cuda.Stream(device=dev)
-    res = {}
-
-    # plain GPU form: one transform, default options (reference heuristic planning)
-    plain = fg.Plan(1, N_MODES, n_trans=1, eps=TOL, dtype="complex64",
-                    gpu_stream=stream.cuda_stream, **plan_kw)
-    t0 = time.perf_counter()
-    plain.setpts(x, y, z)
-    torch.cuda.synchronize()
-    setpts_s = time.perf_counter() - t0
-    fk1 = torch.empty(N_MODES, dtype=torch.complex64, device=dev)
     c0 = c[0].contiguous()
-    ms_plain = time_steps(lambda: plain.execute(c0, out=fk1), stream, args.steps, args.warmup)
-    plain.stage_times(True)
-    plain.execute(c0, out=fk1)
-    torch.cuda.synchronize()
-    st = plain.stage_times(True)
-    info = plain.info()
+
+    def single(kw):
+        p = fg.Plan(1, N_MODES, n_trans=1, eps=TOL, dtype="complex64",
+                    gpu_stream=stream.cuda_stream, **kw)
+        t0 = time.perf_counter()
+        p.setpts(x, y, z)
+        torch.cuda.synchronize()
+        ts = time.perf_counter() - t0
+        f = torch.empty(N_MODES, dtype=torch.complex64, device=dev)
+        ms = time_steps(lambda: p.execute(c0, out=f), stream, args.steps, args.warmup)
+        p.stage_times(True)
+        p.execute(c0, out=f)
+        torch.cuda.synchronize()
+        st = p.stage_times(True)
+        info = p.info()
+        del p
+        torch.cuda.empty_cache()
+        return ms, st, info, ts, f
+
+    # plain GPU form: one transform, the reference library's heuristic planning
+    plain_kw = dict(plan_kw)
+    plain_kw.setdefault("planner", 1)
+    ms_plain, st_plain, info_plain, _, f_plain = single(plain_kw)
     if args.only == "plain":
-        print(json.dumps({"plain_ms": ms_plain, "stage_ms": st, "M": M, "nsub": info.nsub,
-                          "bins": list(info.bins)}))
+        print(json.dumps({"plain_ms": ms_plain, "stage_ms": st_plain, "M": M,
+                          "nsub": info_plain.nsub, "bins": list(info_plain.bins)}))
         return
-    del plain
-    torch.cuda.empty_cache()
+    # this engine's planning, one transform
+    ms_eng, st_eng, info_eng, setpts_s, f_eng = single(plan_kw)
+    if args.only == "engine":
+        print(json.dumps({"engine_ms": ms_eng, "stage_ms": st_eng, "M": M,
+                          "nsub": info_eng.nsub, "bins": list(info_eng.bins)}))
+        return
 
     # planned + batched form: nt vectors sharing the points, graph replay
     torch.cuda.synchronize()
@@ -257,12 +385,10 @@ def run_gpu(args):
     ms_e2e = (time.perf_counter() - t0) * 1e3 / n_e2e
     e2e_err = float(torch.linalg.norm(hf[0].to(dev) - fkb[0]) / torch.linalg.norm(fkb[0]))
     lib.finufftf_destroy(hplan)
+    del hc, hf
 
-    # accuracy on sampled modes against an FP64 direct sum (GPU, torch FP64)
-    err = sampled_error(x, y, z, c[0], fkb[0], dev, nsample=args.err_modes, seed=5)
-
-    # roofline of the dominant kernel (spread): shared-memory atomic updates
-    ns = info.ns
+    # roofline of the dominant kernel (spread): shared-memory adds
+    ns = binfo.ns
     atom_per_launch = float(M) * nt * 2 * ns ** 3
     spread_ms = stb[0]
     achieved = atom_per_launch / (spread_ms * 1e-3)
@@ -284,27 +410,55 @@ def run_gpu(args):
     if rank != 0:
         dist.barrier() if world > 1 else None
         return
+
+    # accuracy: 1e3 sampled modes against an FP64 direct sum, and the CPU
+    # restatement of FINUFFT (same inputs, same tol), which is also the timed
+    # CPU baseline (one execute of one vector over all points)
+    ax = sample_axes(N_MODES, 10, 5)
+    ref = direct_type1_grid([x, y, z], c0, N_MODES, ax, +1, dev)
+    acc = {"batched": rel_l2(take_grid(fkb[0], ax), ref),
+           "plain": rel_l2(take_grid(f_plain, ax), ref),
+           "plain_engine": rel_l2(take_grid(f_eng, ax), ref)}
+    del f_plain, f_eng
+    cpu_line = None
+    if not args.no_cpu and world == 1:
+        del bplan
+        torch.cuda.empty_cache()
+        f_cpu, cs, ce, thr = cpu_type1_3d(np.stack([hx, hy, hz]), c0.cpu().numpy(), TOL,
+                                          np.complex64)
+        acc["cpu"] = rel_l2(take_grid(f_cpu, ax), ref)
+        cpu_line = {"value": M / ce, "unit": "NU pts/s", "cores": thr, "kind": "port",
+                    "sample": "one execute (spread, FFT, deconvolution) of one strength vector "
+                              "over all %d points of the metric workload, timed in full "
+                              "(%.2f s; setpts sort %.2f s outside)" % (M, ce, cs),
+                    "execute_s": ce, "setpts_s": cs}
     value = job_value(M * nt, world, ms_batched)
     out = {
         "metric": METRIC, "value": value, "unit": "NU pts/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batched,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded clustered points, N(0,1) strengths)",
-        "config": {"workload": "3D type 1, 256^3 modes, M=1e8 clustered (8 Gaussians sigma 0.3 "
-                               "+ 20% uniform), complex64, tol 1e-5, iflag +1",
-                   "ntransf_batched": nt, "M": M, "N": list(N_MODES),
+        "config": {"workload": WORKLOAD, "ntransf_batched": nt, "M": M, "N": list(N_MODES),
                    "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas",
-                   "ns": ns, "nf": list(info.nf), "bins": list(info.bins),
-                   "nsub": info.nsub},
+                   "ns": ns, "nf": list(binfo.nf), "bins": list(binfo.bins),
+                   "nsub": binfo.nsub, "kernel": "PSWF" if binfo.kernel_form == 2 else "ES"},
         "plain": {"value": job_value(M, world, ms_plain), "ms_per_step": ms_plain,
-                  "stage_ms": {"spread": st[0], "fft": st[1], "deconv": st[2]}},
+                  "planner": "reference heuristic (cuFINUFFT 2.6: ES kernel, method 2, "
+                             "bins from the shared-memory budget, 1024-point subproblems)",
+                  "stage_ms": {"spread": st_plain[0], "fft": st_plain[1], "deconv": st_plain[2]},
+                  "bins": list(info_plain.bins), "spread_variant": info_plain.spread_variant},
+        "value_over_plain": ms_plain * nt / ms_batched,
+        "plain_engine": {"value": job_value(M, world, ms_eng), "ms_per_step": ms_eng,
+                         "stage_ms": {"spread": st_eng[0], "fft": st_eng[1], "deconv": st_eng[2]}},
         "batched_stage_ms": {"spread": stb[0], "fft": stb[1], "deconv": stb[2]},
         "setpts_s": setpts_s,
         # the reference perftest's amortized figure (perftest/cuda/cuperftest.cu:401):
         # points over makeplan + setpts + one execute, batched plan
         "amortized": {"value": job_value(M * nt, world, (makeplan_s + bsetpts_s) * 1e3 + ms_batched),
                       "unit": "NU pts/s", "makeplan_s": makeplan_s, "setpts_s": bsetpts_s},
-        "rel_l2_err_sampled": err,
+        "accuracy": {"rel_l2_vs_fp64_direct": acc,
+                     "sample": "1e3 modes: seeded 10x10x10 grid of mode indices, vector 0",
+                     "ratio_batched_over_cpu": (acc["batched"] / acc["cpu"]) if "cpu" in acc else None},
         "e2e": {"value": job_value(M * nt, world, ms_e2e), "unit": "NU pts/s",
                 "h2d_bytes_per_step": nt * M * 8, "d2h_bytes_per_step": nt * int(np.prod(N_MODES)) * 8,
                 "api": "finufftf_execute (host pointers, pinned)", "rel_diff_vs_device_api": e2e_err},
@@ -324,268 +478,389 @@ def run_gpu(args):
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "clocks": clk.summary(),
     }
-    if not args.no_cpu and world == 1:
-        out["cpu_baseline"] = cpu_baseline(args.cpu_sample, 1)
+    if cpu_line:
+        out["cpu_baseline"] = cpu_line
+    if not args.no_configs and world == 1:
+        x = y = z = pts = c = c0 = fkb = None
+        torch.cuda.empty_cache()
+        out["configs"] = {}
+        for name in ("c1", "c2", "c4", "c5", "c3f64"):
+            try:
+                out["configs"][name] = CONFIGS[name](args, dev, stream, with_cpu=not args.no_cpu)
+            except Exception as e:  # a failed side config must not hide the metric line
+                out["configs"][name] = {"error": "%s: %s" % (type(e).__name__, e)}
+            torch.cuda.empty_cache()
     print(json.dumps(out))
     if world > 1:
         dist.barrier()
 
 
-# DRAM bytes (read + write) per point per transform of the default 3D spread
-# kernel, from an ncu capture at the same point density (1.25e7 clustered
-# points on a 256^3 grid: 950.2 MB read + 132.4 MB written); scaled by points
-# and transforms to one launch of this workload
-SPREAD_DRAM_BYTES_PER_POINT = (950.213e6 + 132.354e6) / 12.5e6
-
-
-def measured_peak(key):
-    """a peak from MEASURED_PEAKS.json at the repository root (None if absent)"""
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            return float(json.load(f)[key])
-    except (OSError, KeyError, ValueError):
-        return None
-
-
-def sampled_error(x, y, z, c, fk, dev, nsample=64, seed=5):
-    """rel l2 error of nsample modes against an FP64 direct sum on the GPU."""
-    import torch
-
-    g = np.random.default_rng(seed)
-    ks = [g.integers(0, n, nsample) for n in N_MODES]  # row-major indices
-    got = fk[ks[0], ks[1], ks[2]].to(torch.complex128)
-    modes = torch.tensor(np.stack([k - n // 2 for k, n in zip(ks, N_MODES)]),
-                         dtype=torch.float64, device=dev)  # (3, S): axis0 <-> x
-    X = torch.stack([x, y, z]).to(torch.float64)
-    cc = c.to(torch.complex128)
-    ref = torch.zeros(nsample, dtype=torch.complex128, device=dev)
-    chunk = 4_000_000
-    for j0 in range(0, X.shape[1], chunk):
-        ph = modes.T @ X[:, j0:j0 + chunk]
-        ref += (torch.polar(torch.ones_like(ph), ph) * cc[j0:j0 + chunk]).sum(dim=1)
-    return float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
-
-
-def cpu_baseline(m_sample, seed):
-    """CPU restatement of FINUFFT (oracle port) on a bounded sample: the spread
-    of m_sample points is timed and scaled to M=1e8; FFT and deconvolution of
-    the full 512^3 grid are timed as they are."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-
-    pts = clustered_points(m_sample, 1234 + 3).numpy()
-    rng = np.random.default_rng(seed)
-    c = (rng.standard_normal(m_sample) + 1j * rng.standard_normal(m_sample)).astype(np.complex64)
-    plan = O.CpuPlan(1, list(N_MODES), +1, TOL, dtype=np.complex64)
-    plan.setpts([pts[2], pts[1], pts[0]])
-    t0 = time.perf_counter()
-    plan.execute(c)
-    t_full = time.perf_counter() - t0
-    # isolate the spread share: run again with no points to time FFT + deconvolution
-    empty = O.CpuPlan(1, list(N_MODES), +1, TOL, dtype=np.complex64)
-    empty.setpts([np.zeros(1, np.float32)] * 3)
-    t0 = time.perf_counter()
-    empty.execute(np.zeros(1, np.complex64))
-    t_fixed = time.perf_counter() - t0
-    t_spread = max(t_full - t_fixed, 1e-9)
-    t_est = t_spread * (M_FULL / m_sample) + t_fixed
-    return {"value": M_FULL / t_est, "unit": "NU pts/s", "cores": plan.threads, "kind": "port",
-            "sample": "spread of %d clustered points timed and scaled to 1e8; 512^3 FFT + "
-                      "deconvolution timed in full (%.2f s spread, %.2f s fixed)"
-                      % (m_sample, t_spread, t_fixed)}
-
-
-def _timed(fn, stream, steps, warmup):
-    return time_steps(fn, stream, steps, warmup)
-
-
-def run_config(args):
-    """Secondary configurations (one JSON line each; not the metric line)."""
+# ------------------------------------------------------ the other workloads ----
+def cfg_c1(args, dev, stream, with_cpu=True):
+    """C1: 1D type 1 FP64, M = N = 1e6, tol 1e-9 (the reference's CPU-runnable case)"""
     import torch
 
     import finufft_gb300 as fg
 
-    dev = torch.device("cuda", 0)
-    stream = torch.cuda.Stream(device=dev)
+    M, N, tol = 1_000_000, 1_000_000, 1e-9
     g = torch.Generator(device="cuda").manual_seed(11)
-    out = {"config_name": args.config, "n_gpus": 1, "data": "synthetic (seeded)"}
-    if args.config == "c1":
-        # 1D type 1, FP64: M = N = 1e6, tol 1e-9
-        M, N = 1_000_000, 1_000_000
-        x = (torch.rand(M, generator=g, device="cuda", dtype=torch.float64) * 2 - 1) * np.pi
-        c = torch.randn(M, 2, generator=g, device="cuda", dtype=torch.float64).view(torch.complex128)[:, 0]
-        p = fg.Plan(1, (N,), eps=1e-9, dtype="complex128", gpu_stream=stream.cuda_stream)
-        p.setpts(x)
-        f = torch.empty(N, dtype=torch.complex128, device=dev)
-        ms = _timed(lambda: p.execute(c, out=f), stream, args.steps, args.warmup)
-        out.update({"workload": "1D type 1 FP64, M=N=1e6, tol 1e-9", "value": M / (ms * 1e-3),
-                    "unit": "NU pts/s", "ms_per_step": ms})
-    elif args.config == "c2":
-        # 2D type 2 batched: N = 1024^2, ntransf 16, M = 1e7, tol 1e-5, iflag -1
-        M, nt, N = 10_000_000, 16, (1024, 1024)
-        x, y = ((torch.rand(2, M, generator=g, device="cuda", dtype=torch.float64) * 2 - 1)
-                * np.pi).to(torch.float32)
-        fk = torch.randn(nt, *N, 2, generator=g, device="cuda").view(torch.complex64)[..., 0]
-        p1 = fg.Plan(2, N, eps=1e-5, isign=-1, gpu_stream=stream.cuda_stream)
-        p1.setpts(x, y)
-        c1 = torch.empty(M, dtype=torch.complex64, device=dev)
-        f0 = fk[0].contiguous()
-        ms1 = _timed(lambda: p1.execute(f0, out=c1), stream, args.steps, args.warmup)
-        pb = fg.Plan(2, N, n_trans=nt, eps=1e-5, isign=-1, gpu_stream=stream.cuda_stream,
-                     gpu_maxbatchsize=nt)
-        pb.setpts(x, y)
-        cb = torch.empty(nt, M, dtype=torch.complex64, device=dev)
-        pb.execute(fk, out=cb)
-        torch.cuda.synchronize()
-        pb.graph_capture(cb, fk)
-        msb = _timed(pb.graph_launch, stream, args.steps, args.warmup)
-        pb.stage_times(True)
-        pb.execute(fk, out=cb)
-        torch.cuda.synchronize()
-        st = pb.stage_times(True)
-        # interp roofline: grid bytes read per transform + coordinates + output
-        nf = pb.info().nf
-        interp_bytes = nt * nf[0] * nf[1] * 8 + M * 2 * 4 + nt * M * 8
-        out.update({"workload": "2D type 2 FP32, N=1024^2, 16 vectors, M=1e7, tol 1e-5",
-                    "value": M * nt / (msb * 1e-3), "unit": "NU pts/s", "ms_per_step": msb,
-                    "plain": {"value": M / (ms1 * 1e-3), "ms_per_step": ms1},
-                    "batched_stage_ms": {"interp": st[0], "fft": st[1], "amplify": st[2],
-                                         "total": st[3]},
-                    "interp_hbm_GBps_algorithmic": interp_bytes / (st[0] * 1e-3) / 1e9})
-    elif args.config == "c4":
-        # 4096 uneven 2D type 1 problems, tol 1e-6, one batched plan
-        import ctypes
-
-        rng = np.random.default_rng(4)
-        nprob = 4096
-        Ns = np.round(np.exp(rng.uniform(np.log(32), np.log(256), (nprob, 2)))).astype(np.int64)
-        Ms = np.round(np.exp(rng.uniform(np.log(1e3), np.log(1e5), nprob))).astype(np.int64)
-        Mt = int(Ms.sum())
-        xy = ((torch.rand(2, Mt, generator=g, device="cuda", dtype=torch.float64) * 2 - 1)
-              * np.pi).to(torch.float32)
-        c = torch.randn(Mt, 2, generator=g, device="cuda").view(torch.complex64)[:, 0]
-        nm = np.concatenate([Ns, np.ones((nprob, 1), np.int64)], axis=1).ravel()
-        lib = fg.load_library()
-        plan = ctypes.c_void_p()
-        from finufft_gb300 import _lib
-
-        o = _lib.default_opts()
-        o.gpu_stream = stream.cuda_stream
-        assert lib.cufinufftf_batch_makeplan(1, 2, nprob, nm.ctypes.data_as(
-            ctypes.POINTER(ctypes.c_int64)), 1, 1e-6, ctypes.byref(plan), ctypes.byref(o), None) == 0
+    x = (torch.rand(M, generator=g, device="cuda", dtype=torch.float64) * 2 - 1) * np.pi
+    c = torch.randn(M, 2, generator=g, device="cuda", dtype=torch.float64).view(torch.complex128)[:, 0]
+    p = fg.Plan(1, (N,), eps=tol, dtype="complex128", gpu_stream=stream.cuda_stream)
+    p.setpts(x)
+    f = torch.empty(N, dtype=torch.complex128, device=dev)
+    ms = time_steps(lambda: p.execute(c, out=f), stream, args.steps, args.warmup)
+    ax = sample_axes((N,), 1000, 7)
+    ref = direct_type1_grid([x], c, (N,), ax, +1, dev)
+    out = {"workload": "1D type 1 FP64, M=N=1e6 uniform, tol 1e-9", "value": M / (ms * 1e-3),
+           "unit": "NU pts/s", "ms_per_step": ms}
+    gerr = rel_l2(take_grid(f, ax), ref)
+    cerr = None
+    if with_cpu:
+        O = _oracle()
+        cp = O.CpuPlan(1, [N], +1, tol, dtype=np.complex128)
+        cp.setpts([x.cpu().numpy()])
         t0 = time.perf_counter()
-        assert lib.cufinufftf_batch_setpts(plan, Ms.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
-                                           xy[0].data_ptr(), xy[1].data_ptr(), None) == 0
-        torch.cuda.synchronize()
-        setpts_s = time.perf_counter() - t0
-        fk = torch.empty(int((Ns[:, 0] * Ns[:, 1]).sum()), dtype=torch.complex64, device=dev)
-        ms = _timed(lambda: lib.cufinufftf_batch_execute(plan, c.data_ptr(), fk.data_ptr()),
-                    stream, args.steps, args.warmup)
-        lib.cufinufftf_batch_destroy(plan)
-        # per-problem times: a sample of problems run alone through single plans
-        per = []
-        off = np.concatenate([[0], np.cumsum(Ms)])
-        for pidx in rng.choice(nprob, size=min(256, nprob), replace=False):
-            a, b = off[pidx], off[pidx + 1]
-            sp = fg.Plan(1, (int(Ns[pidx, 1]), int(Ns[pidx, 0])), eps=1e-6,
-                         gpu_stream=stream.cuda_stream)
-            sp.setpts(xy[1, a:b].contiguous(), xy[0, a:b].contiguous())
-            cc = c[a:b].contiguous()
-            per.append(_timed(lambda: sp.execute(cc), stream, 3, 1))
-        out.update({"workload": "4096 uneven 2D type 1 FP32, N/side log-uniform [32,256], M "
-                                "log-uniform [1e3,1e5], tol 1e-6, one batched plan",
-                    "value": Mt / (ms * 1e-3), "unit": "NU pts/s", "ms_per_step": ms,
-                    "M_total": Mt, "setpts_s": setpts_s,
-                    "per_problem_ms_single_plans": {"p50": float(np.percentile(per, 50)),
-                                                    "p99": float(np.percentile(per, 99)),
-                                                    "sample": len(per)},
-                    "batched_ms_per_problem": ms / nprob})
-    elif args.config == "c3t2":
-        # 3D type 2 on the metric's points and sizes (the adjoint direction)
-        M = args.m
-        pts = clustered_points(M, 1234 + 3, rng_dev="cuda")
-        fk = torch.randn(*N_MODES, 2, generator=g, device="cuda").view(torch.complex64)[..., 0]
-        p = fg.Plan(2, N_MODES, eps=TOL, isign=-1, gpu_stream=stream.cuda_stream)
-        p.setpts(pts[0].contiguous(), pts[1].contiguous(), pts[2].contiguous())
+        fc = cp.execute(c.cpu().numpy())
+        out["cpu_value"] = M / (time.perf_counter() - t0)
+        out["cpu_cores"] = cp.threads
+        cerr = rel_l2(take_grid(fc, ax), ref)
+    out["accuracy"] = acc_entry(gerr, cerr, "1e3 sampled modes, FP64 direct sum")
+    return out
+
+
+def cfg_c2(args, dev, stream, with_cpu=True):
+    """C2: 2D type 2 FP32, N = 1024^2, 16 vectors, M = 1e7, tol 1e-5, iflag -1"""
+    import torch
+
+    import finufft_gb300 as fg
+
+    M, nt, N, tol = 10_000_000, 16, (1024, 1024), 1e-5
+    g = torch.Generator(device="cuda").manual_seed(12)
+    x, y = ((torch.rand(2, M, generator=g, device="cuda", dtype=torch.float64) * 2 - 1)
+            * np.pi).to(torch.float32)
+    fk = torch.randn(nt, *N, 2, generator=g, device="cuda").view(torch.complex64)[..., 0]
+    f0 = fk[0].contiguous()
+
+    def single(kw):
+        p = fg.Plan(2, N, eps=tol, isign=-1, gpu_stream=stream.cuda_stream, **kw)
+        p.setpts(x, y)
         cc = torch.empty(M, dtype=torch.complex64, device=dev)
-        ms = _timed(lambda: p.execute(fk, out=cc), stream, args.steps, args.warmup)
-        p.stage_times(True)
-        p.execute(fk, out=cc)
-        torch.cuda.synchronize()
-        st = p.stage_times(True)
-        out.update({"workload": "3D type 2 FP32, 256^3 modes, M=1e8 clustered, tol 1e-5",
-                    "value": M / (ms * 1e-3), "unit": "NU pts/s", "ms_per_step": ms,
-                    "stage_ms": {"interp": st[0], "fft": st[1], "amplify": st[2]}})
-    elif args.config == "c3f64":
-        # the metric's workload in double precision at tol 1e-12 (ns = 13)
-        M = args.m
-        pts = clustered_points(M, 1234 + 3, rng_dev="cuda").to(torch.float64)
-        gd = torch.Generator(device="cuda").manual_seed(99)
-        c = torch.randn(M, 2, generator=gd, device="cuda", dtype=torch.float64).view(torch.complex128)[:, 0]
-        x, y, z = (pts[d].contiguous() for d in range(3))
-        p = fg.Plan(1, N_MODES, eps=1e-12, dtype="complex128", gpu_stream=stream.cuda_stream)
-        p.setpts(x, y, z)
-        f = torch.empty(N_MODES, dtype=torch.complex128, device=dev)
-        ms = _timed(lambda: p.execute(c, out=f), stream, min(args.steps, 3), min(args.warmup, 1))
-        p.stage_times(True)
-        p.execute(c, out=f)
-        torch.cuda.synchronize()
-        st = p.stage_times(True)
-        err = sampled_error(x, y, z, c, f, dev, nsample=32, seed=5)
-        info = p.info()
-        out.update({"workload": "3D type 1 FP64, 256^3 modes, M=1e8 clustered, tol 1e-12",
-                    "value": M / (ms * 1e-3), "unit": "NU pts/s", "ms_per_step": ms,
-                    "stage_ms": {"spread": st[0], "fft": st[1], "deconv": st[2]},
-                    "rel_l2_err_sampled": err, "ns": info.ns, "spread_variant": info.spread_variant})
-    elif args.config == "c5":
-        # 3D type 3: M = K = 1e7, sources in box (1,2,4), targets in box (200,100,50)
-        M = K = 10_000_000
-        hs = torch.tensor([1.0, 2.0, 4.0], device="cuda", dtype=torch.float64)[:, None]
-        ht = torch.tensor([200.0, 100.0, 50.0], device="cuda", dtype=torch.float64)[:, None]
-        xs = ((torch.rand(3, M, generator=g, device="cuda", dtype=torch.float64) * 2 - 1) * hs).to(torch.float32)
-        ss = ((torch.rand(3, K, generator=g, device="cuda", dtype=torch.float64) * 2 - 1) * ht).to(torch.float32)
-        c = torch.randn(M, 2, generator=g, device="cuda").view(torch.complex64)[:, 0]
-        p = fg.Plan(3, 3, eps=1e-6, gpu_stream=stream.cuda_stream)
+        ms = time_steps(lambda: p.execute(f0, out=cc), stream, args.steps, args.warmup)
+        return ms, cc
+
+    ms_plain, c_plain = single({"planner": 1})
+    ms1, c1 = single({})
+    pb = fg.Plan(2, N, n_trans=nt, eps=tol, isign=-1, gpu_stream=stream.cuda_stream,
+                 gpu_maxbatchsize=nt)
+    pb.setpts(x, y)
+    cb = torch.empty(nt, M, dtype=torch.complex64, device=dev)
+    pb.execute(fk, out=cb)
+    torch.cuda.synchronize()
+    pb.graph_capture(cb, fk)
+    msb = time_steps(pb.graph_launch, stream, args.steps, args.warmup)
+    pb.stage_times(True)
+    pb.execute(fk, out=cb)
+    torch.cuda.synchronize()
+    st = pb.stage_times(True)
+    nf = pb.info().nf
+    interp_bytes = nt * nf[0] * nf[1] * 8 + M * 2 * 4 + nt * M * 8
+    # accuracy on 1e3 sampled targets, vector 0: c_j = sum_k f_k exp(-i k.x_j)
+    sel = torch.as_tensor(np.random.default_rng(13).choice(M, 1000, replace=False), device=dev)
+    k0 = torch.arange(N[0], dtype=torch.float64, device=dev) - N[0] // 2
+    k1 = torch.arange(N[1], dtype=torch.float64, device=dev) - N[1] // 2
+    one = torch.ones(1, dtype=torch.float64, device=dev)
+    E0 = torch.polar(one, -k0[:, None] * x[sel].to(torch.float64)[None, :])
+    E1 = torch.polar(one, -k1[:, None] * y[sel].to(torch.float64)[None, :])
+    ref = ((f0.to(torch.complex128) @ E1) * E0).sum(0)
+    out = {"workload": "2D type 2 FP32, N=1024^2, 16 vectors, M=1e7 uniform, tol 1e-5",
+           "value": M * nt / (msb * 1e-3), "unit": "NU pts/s", "ms_per_step": msb,
+           "plain": {"value": M / (ms_plain * 1e-3), "ms_per_step": ms_plain,
+                     "planner": "reference heuristic"},
+           "plain_engine": {"value": M / (ms1 * 1e-3), "ms_per_step": ms1},
+           "batched_stage_ms": {"interp": st[0], "fft": st[1], "amplify": st[2], "total": st[3]},
+           "interp_hbm_GBps_algorithmic": interp_bytes / (st[0] * 1e-3) / 1e9}
+    gerr = rel_l2(cb[0][sel], ref)
+    cerr = None
+    if with_cpu:
+        O = _oracle()
+        cp = O.CpuPlan(2, list(N[::-1]), -1, tol, dtype=np.complex64)
+        cp.setpts([y.cpu().numpy(), x.cpu().numpy()])  # fastest axis first
+        cc = cp.execute(f0.cpu().numpy())
+        cerr = rel_l2(cc[sel.cpu().numpy()], ref)
+    out["accuracy"] = acc_entry(gerr, cerr, "1e3 sampled targets of vector 0, FP64 direct sum")
+    out["accuracy"]["plain_rel_l2"] = rel_l2(c_plain[sel], ref)
+    return out
+
+
+def cfg_c4(args, dev, stream, with_cpu=True):
+    """C4: 4096 uneven 2D type-1 FP32 problems in one batched plan, tol 1e-6"""
+    import ctypes
+
+    import torch
+
+    import finufft_gb300 as fg
+    from finufft_gb300 import _lib
+
+    tol = 1e-6
+    g = torch.Generator(device="cuda").manual_seed(14)
+    rng = np.random.default_rng(4)
+    nprob = 4096
+    Ns = np.round(np.exp(rng.uniform(np.log(32), np.log(256), (nprob, 2)))).astype(np.int64)
+    Ms = np.round(np.exp(rng.uniform(np.log(1e3), np.log(1e5), nprob))).astype(np.int64)
+    Mt = int(Ms.sum())
+    xy = ((torch.rand(2, Mt, generator=g, device="cuda", dtype=torch.float64) * 2 - 1)
+          * np.pi).to(torch.float32)
+    c = torch.randn(Mt, 2, generator=g, device="cuda").view(torch.complex64)[:, 0]
+    nm = np.concatenate([Ns, np.ones((nprob, 1), np.int64)], axis=1).ravel()
+    lib = fg.load_library()
+    plan = ctypes.c_void_p()
+    o = _lib.default_opts()
+    o.gpu_stream = stream.cuda_stream
+    assert lib.cufinufftf_batch_makeplan(1, 2, nprob, nm.ctypes.data_as(
+        ctypes.POINTER(ctypes.c_int64)), 1, tol, ctypes.byref(plan), ctypes.byref(o), None) == 0
+    t0 = time.perf_counter()
+    assert lib.cufinufftf_batch_setpts(plan, Ms.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                       xy[0].data_ptr(), xy[1].data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    setpts_s = time.perf_counter() - t0
+    nmodes = Ns[:, 0] * Ns[:, 1]
+    fk = torch.empty(int(nmodes.sum()), dtype=torch.complex64, device=dev)
+    ms = time_steps(lambda: lib.cufinufftf_batch_execute(plan, c.data_ptr(), fk.data_ptr()),
+                    stream, args.steps, args.warmup)
+    lib.cufinufftf_batch_destroy(plan)
+    torch.cuda.synchronize()
+    # per-problem times: a sample of problems run alone through single plans
+    per = []
+    off = np.concatenate([[0], np.cumsum(Ms)])
+    moff = np.concatenate([[0], np.cumsum(nmodes)])
+    for pidx in rng.choice(nprob, size=min(256, nprob), replace=False):
+        a, b = off[pidx], off[pidx + 1]
+        sp = fg.Plan(1, (int(Ns[pidx, 1]), int(Ns[pidx, 0])), eps=tol,
+                     gpu_stream=stream.cuda_stream)
+        sp.setpts(xy[1, a:b].contiguous(), xy[0, a:b].contiguous())
+        cc = c[a:b].contiguous()
+        per.append(time_steps(lambda: sp.execute(cc), stream, 3, 1))
+    out = {"workload": "4096 uneven 2D type 1 FP32, N/side log-uniform [32,256], M "
+                       "log-uniform [1e3,1e5], tol 1e-6, one batched plan",
+           "value": Mt / (ms * 1e-3), "unit": "NU pts/s", "ms_per_step": ms, "M_total": Mt,
+           "setpts_s": setpts_s,
+           "per_problem_ms_single_plans": {"p50": float(np.percentile(per, 50)),
+                                           "p99": float(np.percentile(per, 99)),
+                                           "sample": len(per)},
+           "batched_ms_per_problem": ms / nprob}
+    # accuracy: 64 seeded problems, 16 sampled modes each (1024 modes)
+    fk_h = fk.cpu().numpy()
+    xy_h = xy.cpu().numpy()
+    c_h = c.cpu().numpy()
+    O = _oracle()
+    got, want, cpu = [], [], []
+    for pidx in np.random.default_rng(15).choice(nprob, 64, replace=False):
+        a, b = off[pidx], off[pidx + 1]
+        n0, n1 = int(Ns[pidx, 0]), int(Ns[pidx, 1])  # C order: n0 fastest (pairs with x)
+        kidx = np.random.default_rng(int(pidx)).choice(n0 * n1, 16, replace=False)
+        fprob = fk_h[moff[pidx]:moff[pidx + 1]]
+        ref = O.dirft1([xy_h[0, a:b], xy_h[1, a:b]], c_h[a:b], 1, [n0, n1], kidx=kidx)
+        got.append(fprob[kidx])
+        want.append(ref)
+        if with_cpu:
+            cp = O.CpuPlan(1, [n0, n1], +1, tol, dtype=np.complex64)
+            cp.setpts([xy_h[0, a:b], xy_h[1, a:b]])
+            cpu.append(cp.execute(c_h[a:b]).ravel()[kidx])
+    want = np.concatenate(want)
+    out["accuracy"] = acc_entry(rel_l2(np.concatenate(got), want),
+                                rel_l2(np.concatenate(cpu), want) if cpu else None,
+                                "64 seeded problems x 16 sampled modes, FP64 direct sums")
+    return out
+
+
+def direct_type3(xs, c, ss_sel, isign, dev, chunk=20000):
+    """FP64 direct type-3 sums at a few targets (GPU): f_k = sum_j c_j exp(i isign s_k.x_j)"""
+    import torch
+
+    X = torch.stack([a.to(torch.float64) for a in xs])
+    S = torch.stack([a.to(torch.float64) for a in ss_sel])
+    out = torch.zeros(S.shape[1], dtype=torch.complex128, device=dev)
+    one = torch.ones(1, dtype=torch.float64, device=dev)
+    for j0 in range(0, X.shape[1], chunk):
+        ph = isign * (S.T @ X[:, j0:j0 + chunk])
+        out += torch.polar(one, ph) @ c[j0:j0 + chunk].to(torch.complex128)
+    return out
+
+
+def cfg_c5(args, dev, stream, with_cpu=True):
+    """C5: 3D type 3 FP32, M = K = 1e7, sources in box (1,2,4), targets in box
+    (200,100,50), tol 1e-6; error on 1e4 sampled targets"""
+    import torch
+
+    import finufft_gb300 as fg
+
+    M = K = 10_000_000
+    tol = 1e-6
+    g = torch.Generator(device="cuda").manual_seed(16)
+    hs = torch.tensor([1.0, 2.0, 4.0], device="cuda", dtype=torch.float64)[:, None]
+    ht = torch.tensor([200.0, 100.0, 50.0], device="cuda", dtype=torch.float64)[:, None]
+    xs = ((torch.rand(3, M, generator=g, device="cuda", dtype=torch.float64) * 2 - 1) * hs).to(torch.float32)
+    ss = ((torch.rand(3, K, generator=g, device="cuda", dtype=torch.float64) * 2 - 1) * ht).to(torch.float32)
+    c = torch.randn(M, 2, generator=g, device="cuda").view(torch.complex64)[:, 0]
+    res = {}
+    for name, kw in (("plain", {"planner": 1}), ("engine", {})):
+        p = fg.Plan(3, 3, eps=tol, gpu_stream=stream.cuda_stream, **kw)
         p.setpts(xs[0], xs[1], xs[2], s=ss[0], t=ss[1], u=ss[2])
         f = torch.empty(K, dtype=torch.complex64, device=dev)
-        ms = _timed(lambda: p.execute(c, out=f), stream, args.steps, args.warmup)
-        # error on 256 sampled targets against an FP64 direct sum
-        nchk, blk = 256, 500_000
-        idx = torch.randint(0, K, (nchk,), generator=g, device="cuda")
-        S = ss[:, idx].to(torch.float64)
-        X = xs.to(torch.float64)
-        ref = torch.zeros(nchk, dtype=torch.complex128, device=dev)
-        for j0 in range(0, M, blk):
-            ph = S.T @ X[:, j0:j0 + blk]
-            ref += (torch.polar(torch.ones_like(ph), ph) * c[j0:j0 + blk].to(torch.complex128)).sum(1)
-        err = float(torch.linalg.norm(f[idx].to(torch.complex128) - ref) / torch.linalg.norm(ref))
-        info = p.info()
-        out.update({"workload": "3D type 3 FP32, M=K=1e7, boxes (1,2,4) x (200,100,50), tol 1e-6",
-                    "value": (M + K) / (ms * 1e-3), "unit": "NU pts/s (M+K)", "ms_per_step": ms,
-                    "rel_l2_err_sampled": err, "upsampfac": info.upsampfac, "ns": info.ns,
-                    "nf": list(info.nf), "inner_nf": list(info.inner_nf)})
+        ms = time_steps(lambda: p.execute(c, out=f), stream, args.steps, args.warmup)
+        res[name] = (ms, f, p.info())
+        del p
+    sel = torch.as_tensor(np.random.default_rng(17).choice(K, 10000, replace=False), device=dev)
+    ref = direct_type3([xs[0], xs[1], xs[2]], c, [ss[0][sel], ss[1][sel], ss[2][sel]], +1, dev)
+    ms, f, info = res["engine"]
+    out = {"workload": "3D type 3 FP32, M=K=1e7, boxes (1,2,4) x (200,100,50), tol 1e-6",
+           "value": (M + K) / (ms * 1e-3), "unit": "NU pts/s (M+K)", "ms_per_step": ms,
+           "plain": {"value": (M + K) / (res["plain"][0] * 1e-3), "ms_per_step": res["plain"][0],
+                     "planner": "reference heuristic",
+                     "rel_l2": rel_l2(res["plain"][1][sel], ref)},
+           "upsampfac": info.upsampfac, "ns": info.ns, "nf": list(info.nf),
+           "inner_nf": list(info.inner_nf)}
+    gerr = rel_l2(f[sel], ref)
+    cerr = None
+    if with_cpu:
+        O = _oracle()
+        cp = O.CpuPlan(3, 3, +1, tol, dtype=np.complex64, sigma=info.upsampfac)
+        xh = xs.cpu().numpy()
+        sh = ss.cpu().numpy()
+        cp.setpts([xh[0], xh[1], xh[2]], [sh[0], sh[1], sh[2]])
+        fc = cp.execute(c.cpu().numpy())
+        cerr = rel_l2(fc[sel.cpu().numpy()], ref)
+    out["accuracy"] = acc_entry(gerr, cerr, "1e4 sampled targets, FP64 direct sum")
+    return out
+
+
+def cfg_c3f64(args, dev, stream, with_cpu=True):
+    """C3 in double precision at tol 1e-12: throughput on the full 1e8 points;
+    errors on 1e3 sampled modes of a 1e7-point subset (engine and CPU
+    restatement on the same subset)"""
+    import torch
+
+    import finufft_gb300 as fg
+
+    M = args.m
+    pts = clustered_points(M, 1234 + 3, rng_dev="cuda").to(torch.float64)
+    gd = torch.Generator(device="cuda").manual_seed(99)
+    c = torch.randn(M, 2, generator=gd, device="cuda", dtype=torch.float64).view(torch.complex128)[:, 0]
+    x, y, z = (pts[d].contiguous() for d in range(3))
+    p = fg.Plan(1, N_MODES, eps=1e-12, dtype="complex128", gpu_stream=stream.cuda_stream)
+    p.setpts(x, y, z)
+    f = torch.empty(N_MODES, dtype=torch.complex128, device=dev)
+    ms = time_steps(lambda: p.execute(c, out=f), stream, min(args.steps, 3), min(args.warmup, 1))
+    p.stage_times(True)
+    p.execute(c, out=f)
+    torch.cuda.synchronize()
+    st = p.stage_times(True)
+    info = p.info()
+    out = {"workload": "3D type 1 FP64, 256^3 modes, M=1e8 clustered, tol 1e-12",
+           "value": M / (ms * 1e-3), "unit": "NU pts/s", "ms_per_step": ms,
+           "stage_ms": {"spread": st[0], "fft": st[1], "deconv": st[2]}, "ns": info.ns,
+           "spread_variant": info.spread_variant}
+    # accuracy on a subset (the CPU restatement at ns=13 in FP64 is slow on 1e8)
+    ms_sub = min(M, 10_000_000)
+    xs_, ys_, zs_, cs_ = x[:ms_sub].contiguous(), y[:ms_sub].contiguous(), z[:ms_sub].contiguous(), c[:ms_sub].contiguous()
+    del p
+    ps = fg.Plan(1, N_MODES, eps=1e-12, dtype="complex128", gpu_stream=stream.cuda_stream)
+    ps.setpts(xs_, ys_, zs_)
+    fs = ps.execute(cs_)
+    torch.cuda.synchronize()
+    ax = sample_axes(N_MODES, 10, 5)
+    ref = direct_type1_grid([xs_, ys_, zs_], cs_, N_MODES, ax, +1, dev)
+    gerr = rel_l2(take_grid(fs, ax), ref)
+    del ps, fs, f
+    torch.cuda.empty_cache()
+    cerr = None
+    if with_cpu:
+        fc, _, _, _ = cpu_type1_3d(np.stack([a.cpu().numpy() for a in (xs_, ys_, zs_)]),
+                                   cs_.cpu().numpy(), 1e-12, np.complex128)
+        cerr = rel_l2(take_grid(fc, ax), ref)
+    out["accuracy"] = acc_entry(gerr, cerr, "1e3 modes (10x10x10 grid) of the first %d points"
+                                % ms_sub)
+    return out
+
+
+def cfg_c3t2(args, dev, stream, with_cpu=True):
+    """3D type 2 on the metric's points and sizes (the adjoint direction)"""
+    import torch
+
+    import finufft_gb300 as fg
+
+    M = args.m
+    pts = clustered_points(M, 1234 + 3, rng_dev="cuda")
+    g = torch.Generator(device="cuda").manual_seed(18)
+    fk = torch.randn(*N_MODES, 2, generator=g, device="cuda").view(torch.complex64)[..., 0]
+    p = fg.Plan(2, N_MODES, eps=TOL, isign=-1, gpu_stream=stream.cuda_stream)
+    p.setpts(pts[0].contiguous(), pts[1].contiguous(), pts[2].contiguous())
+    cc = torch.empty(M, dtype=torch.complex64, device=dev)
+    ms = time_steps(lambda: p.execute(fk, out=cc), stream, args.steps, args.warmup)
+    p.stage_times(True)
+    p.execute(fk, out=cc)
+    torch.cuda.synchronize()
+    st = p.stage_times(True)
+    return {"workload": "3D type 2 FP32, 256^3 modes, M=1e8 clustered, tol 1e-5",
+            "value": M / (ms * 1e-3), "unit": "NU pts/s", "ms_per_step": ms,
+            "stage_ms": {"interp": st[0], "fft": st[1], "amplify": st[2]}}
+
+
+CONFIGS = {"c1": cfg_c1, "c2": cfg_c2, "c4": cfg_c4, "c5": cfg_c5, "c3f64": cfg_c3f64,
+           "c3t2": cfg_c3t2}
+
+
+def run_config(args):
+    """One secondary configuration as its own JSON line (not the metric line)."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    out = {"config_name": args.config, "n_gpus": 1, "data": "synthetic (seeded)"}
+    out.update(CONFIGS[args.config](args, dev, stream, with_cpu=not args.no_cpu))
     print(json.dumps(out))
 
 
+# -------------------------------------------------------------- reference arm ----
 def run_reference(args):
-    """CPU FINUFFT restatement on the host cores, same metric and config."""
+    """CPU FINUFFT restatement on the host cores, same metric and workload: each
+    step is one execute of one strength vector over all 1e8 points."""
     rank, world, local = dist_info()
     if rank != 0:
         return
-    vals = []
-    for s in range(args.warmup + args.steps):
-        cb = cpu_baseline(args.cpu_sample, s)
-        if s >= args.warmup:
-            vals.append(cb)
-    v = float(np.median([c["value"] for c in vals]))
+    import torch
+
+    O = _oracle()
+    M = args.m
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    pts = clustered_points(M, 1234 + 3, rng_dev=dev).cpu().numpy()
+    c0 = strengths(1, M, 99, dev)[0].cpu().numpy()
+    plan = O.CpuPlan(1, list(N_MODES[::-1]), +1, TOL, dtype=np.complex64)
+    t0 = time.perf_counter()
+    plan.setpts([pts[2], pts[1], pts[0]])
+    setpts_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        plan.execute(c0)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        plan.execute(c0)
+        times.append(time.perf_counter() - t0)
+    ms = float(np.mean(times)) * 1e3
+    v = M / (ms * 1e-3)
     out = {"metric": METRIC, "value": v, "unit": "NU pts/s", "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": M_FULL / v * 1e3, "higher_is_better": True,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
            "data": "synthetic (seeded clustered points, N(0,1) strengths)",
-           "config": {"workload": "3D type 1, 256^3 modes, M=1e8 clustered (8 Gaussians sigma 0.3 "
-                                  "+ 20% uniform), complex64, tol 1e-5, iflag +1"},
-           "cpu_baseline": {"kind": "port", "cores": vals[-1]["cores"], "sample": vals[-1]["sample"],
+           "config": {"workload": WORKLOAD, "M": M, "N": list(N_MODES), "ntransf_per_step": 1,
+                      "parallelism": "host cores (OpenMP)"},
+           "cpu_baseline": {"kind": "port", "cores": plan.threads,
+                            "sample": "every step: one execute (spread, FFT, deconvolution) of "
+                                      "one strength vector over all %d points; setpts sort "
+                                      "%.2f s outside the steps" % (M, setpts_s),
                             "value": v, "unit": "NU pts/s"},
+           "step_s": {"min": min(times), "max": max(times), "median": float(np.median(times))},
            "e2e": {"value": v, "unit": "NU pts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -598,18 +873,17 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--m", type=int, default=M_FULL)
     ap.add_argument("--ntransf", type=int, default=4)
-    ap.add_argument("--cpu-sample", type=int, default=4_000_000)
-    ap.add_argument("--err-modes", type=int, default=32)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU restatement legs")
+    ap.add_argument("--no-configs", action="store_true", help="skip the nested workloads")
     ap.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c3f64", "c3t2", "c4", "c5"],
                     help="c3 (default) is the metric line; the others print their own line")
     ap.add_argument("--nmodes", type=int, default=0, help="modes per side (profiling cases)")
     ap.add_argument("--bins", default="", help="bin sizes x,y,z (default: the planner's)")
     ap.add_argument("--maxsub", type=int, default=0, help="max points per subproblem")
     ap.add_argument("--variant", type=int, default=-1, help="3D spread variant (tuning runs)")
-    ap.add_argument("--planner", type=int, default=0, help="1: reference heuristic planning")
-    ap.add_argument("--only", default="", choices=["", "plain"],
-                    help="plain: time only the single-transform plan (profiling runs)")
+    ap.add_argument("--planner", type=int, default=0, help="planner of the engine's forms")
+    ap.add_argument("--only", default="", choices=["", "plain", "engine"],
+                    help="time only the single-transform plan of that form (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -100,6 +100,8 @@ template <typename T> struct PointLayout {
   // its results in sorted order here and a scatter pass per transform moves
   // them to user order, so the scattered writes of one transform merge in L2
   void *sorted_out = nullptr;
+  // interpolation schedule: 0 auto, 1 gather per point, 2 shared-memory tiles
+  int interp_mode = 0;
 };
 
 } // namespace gbn

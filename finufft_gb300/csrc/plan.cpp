@@ -174,8 +174,7 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
   // larger subproblems amortise the tile clear and write-back (measured on the
   // 1e8-point clustered 512^3 case: 16x12x8 bins, 4096-point subproblems)
   const bool v3_default = dim == 3 && ext.planner == 0 && std::is_same_v<T, float> && ns <= 8 &&
-                          (ext.spread_variant < 0 || ext.spread_variant == 3) &&
-                          !std::getenv("GBNUFFT_SPREAD_VARIANT");
+                          (ext.spread_variant < 0 || ext.spread_variant == 3);
   if (v3_default) {
     defb[0] = 16;
     defb[1] = ns <= 6 ? 12 : 8;
@@ -215,7 +214,6 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
     // per tile with runs added by atomics
     int variant = ext.planner == 1 ? 0 : 2;
     if (ext.spread_variant >= 0) variant = ext.spread_variant;
-    if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT")) variant = std::atoi(e);
     if (variant < 0 || variant > 2) variant = 0;
     const int warps2 = variant == 1 ? 1 : 8;
     const size_t sm2 = spread_tile2m_bytes<T>(ns, bins, warps2);
@@ -240,7 +238,6 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
     const bool v3ok = std::is_same_v<T, float> ? ns <= 8 : ns <= 5;
     int variant = ext.planner == 1 ? 0 : (v3ok ? 3 : (ns <= 8 ? 2 : 0));
     if (ext.spread_variant >= 0) variant = ext.spread_variant;
-    if (const char *e = std::getenv("GBNUFFT_SPREAD_VARIANT")) variant = std::atoi(e);
     if (variant == 1 && wsm > (size_t)limit) variant = 2;
     if (variant < 0 || variant > 3 || (variant >= 2 && ns > 8)) variant = 0;
     if (variant == 3) {
@@ -373,6 +370,7 @@ template <typename T> PointLayout<T> Plan<T>::layout() const {
   L.perm = perm.p;
   L.cell_sorted = cell_sorted;
   L.sorted_out = isort.p;
+  L.interp_mode = ext.interp_mode;
   return L;
 }
 
@@ -390,10 +388,9 @@ void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]
   uint64_t sbinvol = 1;
   for (int d = 0; d < dim; ++d) sbinvol *= (uint64_t)bins[d] + 1;
   int cell_keys = (uint64_t)nb * binvol0 <= 0xffffffffull ? 1 : 0;
-  // GBNUFFT_START_CELL_KEYS=0 keeps whole-cell keys (tuning comparisons)
-  const char *hc = std::getenv("GBNUFFT_START_CELL_KEYS");
+  // gbnufft_opts.sort_keys = 1 keeps whole-cell keys for odd widths too
   if (cell_keys && K.ns % 2 == 1 && (uint64_t)nb * sbinvol <= 0xffffffffull &&
-      !(hc && std::atoi(hc) == 0))
+      ext.sort_keys != 1)
     cell_keys = 2;
   const uint64_t binvol = cell_keys == 2 ? sbinvol : binvol0;
   cell_sorted = cell_keys ? 1 : 0;
@@ -427,16 +424,21 @@ void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]
   // type 2 batches whose per-transform output fits in L2: interpolate into
   // sorted order, then scatter transform by transform (measured on 16 vectors
   // of 1e7 2D points: 6.3 -> 5.8 ms; the interpolation alone runs at 2.4 ms
-  // once the scattered 8-byte writes are out of it).
-  // GBNUFFT_INTERP_SORTED=0 writes user order directly (tuning comparisons)
+  // once the scattered 8-byte writes are out of it). The sorted copy of a
+  // batch's outputs is only taken when it costs at most an eighth of the
+  // device memory free at setpts. gbnufft_opts.interp_mode 1 or 2 writes user
+  // order directly.
   isort.release();
-  const char *iso = std::getenv("GBNUFFT_INTERP_SORTED");
   if (type == 2 && batchsize > 1 && batchsize <= 65535 && dim >= 2 && M > 0 &&
-      !(iso && std::atoi(iso) == 0)) { // (the scatter's grid has one row per transform)
+      ext.interp_mode == 0) { // (the scatter's grid has one row per transform)
     int dev = 0, l2 = 0;
     GBN_CUDA(cudaGetDevice(&dev));
     GBN_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
-    if ((double)M * sizeof(cplx<T>) <= 0.75 * (double)l2) isort.resize((size_t)batchsize * M);
+    size_t freeb = 0, totb = 0;
+    GBN_CUDA(cudaMemGetInfo(&freeb, &totb));
+    const double bytes = (double)batchsize * M * sizeof(cplx<T>);
+    if ((double)M * sizeof(cplx<T>) <= 0.75 * (double)l2 && bytes <= 0.125 * (double)freeb)
+      isort.resize((size_t)batchsize * M);
   }
 }
 

@@ -1614,11 +1614,8 @@ template <typename T, int DIM> struct Dispatch {
                      int ntr, cudaStream_t s) {
     if constexpr (DIM >= 2) {
       // tile-staged interpolation when one transform's tile fits the per-block
-      // budget (three blocks per SM); GBNUFFT_INTERP_METHOD=0 keeps the gather
-      static const int imethod = [] {
-        const char *e = std::getenv("GBNUFFT_INTERP_METHOD");
-        return e ? std::atoi(e) : 1;
-      }();
+      // budget (three blocks per SM); interp_mode 1 keeps the gather
+      const int imethod = L.interp_mode == 1 ? 0 : 1;
       size_t cells = 1;
       for (int d = 0; d < DIM; ++d) cells *= (size_t)(L.bin[d] + NS);
       const size_t tbytes = cells * sizeof(cplx<T>);

@@ -42,7 +42,12 @@ typedef struct gbnufft_opts {
                          1: ES (src/cuda/makeplan.cu:43-119); 2: PSWF */
   int kerformula;     /* PSWF shape parameter choice as finufft_opts.spread_kerformula:
                          0 or 8 (default), 7, 9; other values are rejected */
-  int reserved[10];
+  int sort_keys;      /* 0 (default): points sorted by bin and, inside the bin, by the
+                         first cell of their kernel support; 1: by bin and cell */
+  int interp_mode;    /* type 2 interpolation: 0 auto; 1 one thread per point gathering
+                         from the grid; 2 shared-memory tiles writing user order directly
+                         (auto may write sorted order and scatter it per transform) */
+  int reserved[8];
 } gbnufft_opts;
 
 typedef struct gbnufft_plan_info {

@@ -9,8 +9,17 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_PY = os.path.join(os.environ.get("FINUFFT_REFERENCE_DIR", "/root/reference"), "python",
-                      "cufinufft")
+
+
+def _reference_dir():
+    """the reference source tree: FINUFFT_REFERENCE_DIR, else the oracle
+    Makefile's default"""
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "print-ref"],
+                       capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
+
+REF_PY = os.path.join(_reference_dir(), "python", "cufinufft")
 LIB_DIR = os.path.join(ROOT, "finufft_gb300", "_build")
 
 PROBE = r"""
