@@ -48,6 +48,8 @@ class PlanInfo(Structure):
         ("M", c_int64), ("N", c_int64), ("spread_smem", c_size_t),
         ("horner_err", c_double), ("inner_nf", c_int * 3), ("spread_variant", c_int),
         ("maxsubprobsize", c_int), ("spread_fixed", c_int), ("kernel_form", c_int),
+        ("planner_used", c_int), ("planned_slot", c_int), ("features", c_float * 12),
+        ("tune_ms", c_double * 12),
     ]
 
 
@@ -160,6 +162,25 @@ def _declare(lib):
     lib.gbnufft_kernel_choice.restype = c_int
     lib.gbnufft_kernel_eval.argtypes = [c_int, c_int, c_double, c_int64, c_void_p, c_void_p]
     lib.gbnufft_kernel_eval.restype = c_int
+    ip = POINTER(c_int)
+    fp = POINTER(c_float)
+    lib.gbnufft_planner_dims.argtypes = [ip, ip, ip, ip]
+    lib.gbnufft_planner_dims.restype = c_int
+    lib.gbnufft_planner_candidate.argtypes = [c_int, c_int, c_int, POINTER(c_double), ip, ip,
+                                              ip, ip]
+    lib.gbnufft_planner_candidate.restype = c_int
+    lib.gbnufft_planner_model.argtypes = [ip, c_void_p, c_void_p, c_void_p, c_void_p,
+                                          c_void_p, fp, fp]
+    lib.gbnufft_planner_model.restype = c_int
+    lib.gbnufft_planner_forward.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p]
+    lib.gbnufft_planner_forward.restype = c_int
+    lib.gbnufft_planner_train.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_int, c_int,
+                                          c_float, c_float, ctypes.c_uint, c_void_p, c_void_p]
+    lib.gbnufft_planner_train.restype = c_int
+    lib.gbnufft_point_features.argtypes = [c_int, c_int, c_int, c_int64, c_void_p, c_void_p,
+                                           c_void_p, c_void_p, c_void_p, c_double, c_double,
+                                           c_int, c_double, c_void_p, c_void_p]
+    lib.gbnufft_point_features.restype = c_int
     for pfx, real in (("finufft", c_double), ("finufftf", c_float)):
         f = getattr(lib, pfx + "_makeplan")
         f.argtypes = [c_int, c_int, i64p, c_int, c_int, real, POINTER(c_void_p),

@@ -30,6 +30,7 @@ CU_SOURCES = [
     "spreadinterp_3d.cu",
     "noalloc.cu",
     "batch.cu",
+    "planner.cu",
 ]
 CPP_SOURCES = ["planning.cpp", "plan.cpp", "c_api.cpp", "host_api.cpp"]
 
@@ -59,7 +60,7 @@ def build(verbose=False, force=False, extra_nvcc=()):
     """Compile every translation unit (in parallel) and link libcufinufft.so."""
     os.makedirs(OUT_DIR, exist_ok=True)
     nvcc = _nvcc()
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".inc"))]
     headers += [os.path.join(INC, f) for f in os.listdir(INC) if f.endswith(".h")]
     common = ["-O3", "-std=c++20", "-I", INC, "-I", CSRC, "-DNDEBUG"]
     jobs = []

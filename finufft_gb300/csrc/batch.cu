@@ -192,7 +192,7 @@ BatchPlan<T>::BatchPlan(int type_, int dim_, int nprob_, const int64_t *modes, i
   const KernelChoice kc =
       form == KERNEL_PSWF
           ? choose_kernel_pswf(tol, opts.upsampfac, dim, type, std::is_same_v<T, float>,
-                               ext.kerformula, 0, opts.debug)
+                               ext.kerformula, 0, 0, opts.debug)
           : choose_kernel(tol, opts.upsampfac, opts.gpu_kerevalmeth, std::is_same_v<T, float>,
                           0, opts.debug);
   build_kernel_shape<T>(make_kernel_fn(form, kc.ns, kc.beta), opts.gpu_kerevalmeth == 1, tol,

@@ -143,6 +143,10 @@ template <typename T> int info_dev(void *p, gbnufft_plan_info *info) {
     info->maxsubprobsize = P.maxsub;
     info->spread_fixed = P.spread_fixed_in_use();
     info->kernel_form = P.K.form;
+    info->planner_used = P.planner_used;
+    info->planned_slot = P.planned_slot;
+    for (int f = 0; f < gbn::PLANNER_NF; ++f) info->features[f] = P.features[f];
+    for (int k = 0; k < gbn::PLANNER_K; ++k) info->tune_ms[k] = P.tune_ms[k];
   });
 }
 
@@ -307,7 +311,7 @@ int gbnufft_kernel_choice(double tol, double sigma, int dim, int type, int is_fl
     if (!ns || !beta) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "ns/beta");
     const gbn::KernelChoice kc =
         form == gbn::KERNEL_PSWF
-            ? gbn::choose_kernel_pswf(tol, sigma, dim, type, is_float, kerformula, 0, 0)
+            ? gbn::choose_kernel_pswf(tol, sigma, dim, type, is_float, kerformula, 0, 0, 0)
             : gbn::choose_kernel(tol, sigma, 0, is_float, 0, 0);
     *ns = kc.ns;
     *beta = kc.beta;
@@ -323,6 +327,87 @@ int gbnufft_kernel_eval(int form, int ns, double beta, int64_t n, const double *
       GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "ns/n");
     const gbn::KernelFn phi = gbn::make_kernel_fn(form, ns, beta);
     for (int64_t i = 0; i < n; ++i) out[i] = phi(x[i]);
+  });
+}
+
+int gbnufft_planner_dims(int *nfeat, int *hidden, int *nslots, int *nweights) {
+  return guarded([&] {
+    if (!nfeat || !hidden || !nslots || !nweights) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "null");
+    *nfeat = gbn::PLANNER_NF;
+    *hidden = gbn::PLANNER_H;
+    *nslots = gbn::PLANNER_K;
+    *nweights = gbn::PLANNER_NW;
+  });
+}
+
+int gbnufft_planner_candidate(int dim, int is_double, int slot, double *sigma, int *bins,
+                              int *maxsub, int *variant, int *reference) {
+  return guarded([&] {
+    gbn::Candidate c;
+    if (!gbn::planner_candidate(dim, is_double != 0, slot, &c))
+      GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "slot");
+    if (sigma) *sigma = c.sigma;
+    if (bins)
+      for (int d = 0; d < 3; ++d) bins[d] = c.bins[d];
+    if (maxsub) *maxsub = c.maxsub;
+    if (variant) *variant = c.variant;
+    if (reference) *reference = c.reference;
+  });
+}
+
+int gbnufft_planner_model(int *trained, float *weights, float *mean, float *stdev, float *lo,
+                          float *hi, float *ymean, float *ystd) {
+  return guarded([&] {
+    const gbn::PlannerModel &m = gbn::planner_model();
+    if (trained) *trained = m.trained ? 1 : 0;
+    if (mean) std::memcpy(mean, m.mean, sizeof(float) * gbn::PLANNER_NF);
+    if (stdev) std::memcpy(stdev, m.stdev, sizeof(float) * gbn::PLANNER_NF);
+    if (lo) std::memcpy(lo, m.lo, sizeof(float) * gbn::PLANNER_NF);
+    if (hi) std::memcpy(hi, m.hi, sizeof(float) * gbn::PLANNER_NF);
+    if (ymean) *ymean = m.ymean;
+    if (ystd) *ystd = m.ystd;
+    if (weights) gbn::planner_weights_host(weights);
+  });
+}
+
+int gbnufft_planner_forward(const float *d_weights, int n, const float *d_x, float *d_y,
+                            void *stream) {
+  return guarded([&] {
+    if (n < 0 || (n > 0 && (!d_weights || !d_x || !d_y)))
+      GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "forward");
+    gbn::mlp_forward(d_weights, n, d_x, d_y, (cudaStream_t)stream);
+  });
+}
+
+int gbnufft_planner_train(int n, const float *x, const float *t, const float *mask, int epochs,
+                          int batch, float lr, float weight_decay, unsigned seed, float *w,
+                          float *loss) {
+  return guarded([&] {
+    if (n < 1 || epochs < 1 || batch < 1 || !x || !t || !mask || !w)
+      GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "train");
+    gbn::mlp_train(n, x, t, mask, epochs, batch, lr, weight_decay, seed, w, loss);
+  });
+}
+
+int gbnufft_point_features(int dim, int type, int is_double, int64_t M, const void *d_x,
+                           const void *d_y, const void *d_z, const double *shift,
+                           const double *scale, double nmodes, double tol, int ntr,
+                           double xs_product, float *feat, void *stream) {
+  return guarded([&] {
+    if (dim < 1 || dim > 3 || M < 0 || !shift || !scale || !feat)
+      GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "features");
+    const cudaStream_t s = (cudaStream_t)stream;
+    if (is_double) {
+      const double *xyz[3] = {(const double *)d_x, (const double *)(dim > 1 ? d_y : d_x),
+                              (const double *)(dim > 2 ? d_z : d_x)};
+      gbn::point_features<double>(dim, type, true, M, xyz, shift, scale, nmodes, tol, ntr,
+                                  xs_product, feat, s);
+    } else {
+      const float *xyz[3] = {(const float *)d_x, (const float *)(dim > 1 ? d_y : d_x),
+                             (const float *)(dim > 2 ? d_z : d_x)};
+      gbn::point_features<float>(dim, type, false, M, xyz, shift, scale, nmodes, tol, ntr,
+                                 xs_product, feat, s);
+    }
   });
 }
 

@@ -94,7 +94,11 @@ int makeplan_host(int type, int dim, const int64_t *n_modes, int iflag, int ntr,
                                               : std::min(8, std::max(1, (ntr + 3) / 4));
     if (fo.spread_max_sp_size > 0) co.gpu_maxsubprobsize = fo.spread_max_sp_size;
     // the CPU library's kernel: the PSWF with its shape choice (any sigma > 1;
-    // the pieces are fitted for the sigma given), spread/interp-only included
+    // the pieces are fitted for the sigma given), spread/interp-only included.
+    // kerevalmeth 0 only lifts the GPU interface's restriction of Horner
+    // evaluation to sigma 2 and 1.25 (the PSWF is always evaluated by Horner)
+    if (fo.upsampfac != 0.0 && fo.upsampfac != 2.0 && fo.upsampfac != 1.25)
+      co.gpu_kerevalmeth = 0;
     gbnufft_opts ext;
     gbnufft_default_opts(&ext);
     ext.kernel_form = gbn::KERNEL_PSWF;

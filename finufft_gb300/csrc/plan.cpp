@@ -10,6 +10,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
+#include <cfloat>
 
 #include "planning.h"
 #include "sort.h"
@@ -83,13 +86,19 @@ Plan<T>::Plan(int type_, int dim_, const int64_t *modes_in, int iflag_, int ntra
   if (opts.gpu_method < 0 || opts.gpu_method > 4) GBN_THROW(FINUFFT_ERR_METHOD_NOTVALID, "method");
   if (opts.gpu_method == 4 && dim != 3) GBN_THROW(FINUFFT_ERR_METHOD_NOTVALID, "method 4 is 3D only");
   stream = (cudaStream_t)opts.gpu_stream;
-  const int form = plan_kernel_form(ext, opts);
+  if (ext.planner < 0 || ext.planner > 3) {
+    fprintf(stderr, "[gbnufft] invalid planner %d (0 engine, 1 reference heuristic, 2 learned, "
+                    "3 autotuned)\n", ext.planner);
+    GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "planner");
+  }
+  form = plan_kernel_form(ext, opts);
   if (type == 3) opts.gpu_spreadinterponly = 1; // the outer type 1 only spreads
   else
     for (int d = 0; d < dim; ++d) ms[d] = (int)modes_in[d];
   nmodes = (int64_t)ms[0] * ms[1] * ms[2];
   batchsize = opts.gpu_maxbatchsize > 0 ? opts.gpu_maxbatchsize : std::min(ntransf, 8);
   if (type == 3) batchsize = std::min(batchsize, ntransf);
+  user_sigma = opts.upsampfac != 0.0;
   if (opts.upsampfac == 0.0) {
     // reference rule (src/cuda/makeplan.cu:289-297): 2, or 1.25 for type 3 at
     // tol >= 1e-9. In single precision sigma 1.25 loses digits to the wide range
@@ -99,27 +108,8 @@ Plan<T>::Plan(int type_, int dim_, const int64_t *modes_in, int iflag_, int ntra
     if (type == 3 && tol >= 1e-9 && (ext.planner == 1 || !f32 || (float)tol >= 1e-4f))
       opts.upsampfac = 1.25;
   }
-  const bool is_float = std::is_same_v<T, float>;
-  const KernelChoice kc =
-      form == KERNEL_PSWF
-          ? choose_kernel_pswf(tol, opts.upsampfac, dim, type, is_float, ext.kerformula,
-                               opts.gpu_spreadinterponly, opts.debug)
-          : choose_kernel(tol, opts.upsampfac, opts.gpu_kerevalmeth, is_float,
-                          opts.gpu_spreadinterponly, opts.debug);
-  horner_err = build_kernel_shape<T>(make_kernel_fn(form, kc.ns, kc.beta),
-                                     opts.gpu_kerevalmeth == 1, tol, &K);
-  if (type != 3) {
-    for (int d = 0; d < dim; ++d)
-      nf[d] = opts.gpu_spreadinterponly ? ms[d]
-                                        : (int)fine_grid_len(ms[d], opts.upsampfac, K.ns);
-    nf_total = (int64_t)nf[0] * nf[1] * nf[2];
-    choose_spread_config(opts.gpu_method != 0);
-    if (!opts.gpu_spreadinterponly) {
-      fw.resize((size_t)nf_total * batchsize);
-      make_fft();
-      make_fseries();
-    }
-  }
+  make_kernel();
+  if (type != 3) make_grid();
   if (opts.debug)
     printf("[gbnufft] type %d dim %d ntr %d: ns=%d beta=%.4g sigma=%.3g nf=(%d,%d,%d) "
            "method=%d bins=(%d,%d,%d) batch=%d horner_err=%.2e\n",
@@ -127,13 +117,48 @@ Plan<T>::Plan(int type_, int dim_, const int64_t *modes_in, int iflag_, int ntra
            method, bins[0], bins[1], bins[2], batchsize, horner_err);
 }
 
+// Kernel width and shape at the plan's tolerance and upsampling factor.
+template <typename T> void Plan<T>::make_kernel() {
+  const bool is_float = std::is_same_v<T, float>;
+  const KernelChoice kc =
+      form == KERNEL_PSWF
+          ? choose_kernel_pswf(tol, opts.upsampfac, dim, type, is_float, ext.kerformula,
+                               user_sigma ? opts.gpu_kerevalmeth : 0, opts.gpu_spreadinterponly,
+                               opts.debug)
+          : choose_kernel(tol, opts.upsampfac, opts.gpu_kerevalmeth, is_float,
+                          opts.gpu_spreadinterponly, opts.debug);
+  horner_err = build_kernel_shape<T>(make_kernel_fn(form, kc.ns, kc.beta),
+                                     opts.gpu_kerevalmeth == 1, tol, &K);
+}
+
+// Types 1/2: fine grid, spread configuration, grid buffers, FFT plan and
+// 1/phihat (again when a planner changes the upsampling factor at setpts).
+template <typename T> void Plan<T>::make_grid() {
+  for (int d = 0; d < dim; ++d)
+    nf[d] = opts.gpu_spreadinterponly ? ms[d] : (int)fine_grid_len(ms[d], opts.upsampfac, K.ns);
+  nf_total = (int64_t)nf[0] * nf[1] * nf[2];
+  choose_spread_config(opts.gpu_method != 0);
+  if (!opts.gpu_spreadinterponly) {
+    destroy_fft();
+    fw.resize((size_t)nf_total * batchsize);
+    make_fft();
+    make_fseries();
+  }
+}
+
+template <typename T> void Plan<T>::destroy_fft() {
+  if (have_fft) cufftDestroy(fftplan);
+  if (fft_x) cufftDestroy(fft_x);
+  if (fft_rest0) cufftDestroy(fft_rest0);
+  if (fft_rest1) cufftDestroy(fft_rest1);
+  have_fft = pruned = false;
+  fftplan = fft_x = fft_rest0 = fft_rest1 = 0;
+}
+
 template <typename T> Plan<T>::~Plan() {
   try {
     DeviceScope ds(opts.gpu_device_id);
-    if (have_fft) cufftDestroy(fftplan);
-    if (fft_x) cufftDestroy(fft_x);
-    if (fft_rest0) cufftDestroy(fft_rest0);
-    if (fft_rest1) cufftDestroy(fft_rest1);
+    destroy_fft();
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
   } catch (...) {
@@ -353,6 +378,188 @@ template <typename T> void Plan<T>::make_fseries() {
   }
 }
 
+// ---------------------------------------------------------- planners 2, 3 ----
+template <typename T> bool Plan<T>::candidate_valid(const Candidate &c) const {
+  // analytic rejection: the PSWF width law's width for tol at this sigma must
+  // fit the precision's widest kernel, so the kernel's aliasing bound reaches tol
+  const bool is_float = std::is_same_v<T, float>;
+  const double t = std::max(tol, is_float ? (double)FLT_EPSILON : DBL_EPSILON);
+  const double tolfac = 0.18 * std::pow(1.4, dim - 1) * (type == 3 ? 1.4 : 1.0);
+  const int ns = (int)std::ceil(std::log(tolfac / t) / (PI * std::sqrt(1.0 - 1.0 / c.sigma)) + 1.0);
+  const int maxns = is_float ? MAX_NS_FLOAT : MAX_NS;
+  return ns <= maxns && kernel_tol_bound(std::max(ns, 2), c.sigma, dim, type) <= t * (1 + 1e-9);
+}
+
+template <typename T> void Plan<T>::apply_sigma(double sigma) {
+  if (sigma == opts.upsampfac) return;
+  opts.upsampfac = sigma;
+  user_sigma = false; // the planner's choice: fitted pieces for any sigma
+  make_kernel();
+  if (type != 3) make_grid();
+}
+
+template <typename T> void Plan<T>::apply_shape(const Candidate &c) {
+  cufinufft_opts o = opts;
+  gbnufft_opts e = ext;
+  if (c.reference) {
+    e.planner = 1;
+    o.gpu_binsizex = o.gpu_binsizey = o.gpu_binsizez = 0;
+    o.gpu_maxsubprobsize = 1024;
+    e.spread_variant = -1;
+  } else {
+    e.planner = 0;
+    o.gpu_binsizex = c.bins[0];
+    o.gpu_binsizey = c.bins[1];
+    o.gpu_binsizez = c.bins[2];
+    o.gpu_maxsubprobsize = c.maxsub;
+    e.spread_variant = c.variant;
+  }
+  o.gpu_method = 0;
+  const SpreadSetup S = spread_setup<T>(dim, K.ns, nf, o, e, false);
+  for (int d = 0; d < 3; ++d) {
+    bins[d] = S.bins[d];
+    nbins[d] = S.nbins[d];
+  }
+  method = S.method;
+  spread_smem = S.smem;
+  scfg = S.cfg;
+  maxsub = S.maxsub;
+}
+
+namespace {
+// autotuner cache: problem class -> chosen slot (process-wide)
+std::mutex tune_mu;
+std::map<std::vector<int>, int> tune_cache;
+} // namespace
+
+template <typename T>
+double Plan<T>::time_candidate(const Candidate &c, int64_t Ms, const T *const xs[3]) {
+  apply_sigma(c.sigma);
+  apply_shape(c);
+  AxisMap ax[3];
+  for (int d = 0; d < 3; ++d) ax[d] = AxisMap{0.0, 1.0, nf[d], bins[d]};
+  sort_points(Ms, xs, ax);
+  const PointLayout<T> L = layout();
+  AsyncBuf cv((size_t)std::max<int64_t>(Ms, 1) * sizeof(cplx<T>), stream);
+  GBN_CUDA(cudaMemsetAsync(cv.p, 0x3c, (size_t)std::max<int64_t>(Ms, 1) * sizeof(cplx<T>),
+                           stream)); // any finite nonzero strengths
+  cudaEvent_t e0, e1, e2;
+  GBN_CUDA(cudaEventCreate(&e0));
+  GBN_CUDA(cudaEventCreate(&e1));
+  GBN_CUDA(cudaEventCreate(&e2));
+  float best = 1e30f, fft_ms = 0;
+  for (int rep = 0; rep < 3; ++rep) {
+    GBN_CUDA(cudaEventRecord(e0, stream));
+    if (type == 1)
+      launch_spread<T>(L, K, cv.as<cplx<T>>(), nullptr, 0, fw.p, nf_total, 1, scfg, stream);
+    else
+      launch_interp<T>(L, K, fw.p, nf_total, nullptr, 0, cv.as<cplx<T>>(), 1, stream);
+    GBN_CUDA(cudaEventRecord(e1, stream));
+    fft(fw.p, 1, type == 1);
+    GBN_CUDA(cudaEventRecord(e2, stream));
+    GBN_CUDA(cudaEventSynchronize(e2));
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, e0, e1);
+    cudaEventElapsedTime(&b, e1, e2);
+    if (rep > 0) { // the first run warms up
+      best = std::min(best, a);
+      fft_ms = b;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  // the sample's spread (or interpolation) scaled to all points, plus the FFT
+  return (double)best * ((double)Mtune / (double)std::max<int64_t>(Ms, 1)) + fft_ms;
+}
+
+template <typename T>
+Candidate Plan<T>::plan_shape(int64_t Mp, const T *const xyz[3], int64_t Np) {
+  const bool dbl = std::is_same_v<T, double>;
+  double shift[3] = {-PI, -PI, -PI}, scale[3] = {0.5 / PI, 0.5 / PI, 0.5 / PI};
+  double xs_product = 0;
+  if (type == 3)
+    for (int d = 0; d < dim; ++d) {
+      const double X = t3X[d] > 0 ? t3X[d] : 1.0;
+      shift[d] = t3C[d] - X;
+      scale[d] = 0.5 / X;
+      xs_product += std::log10(t3X[d] * t3S[d] + 1.0) / dim;
+    }
+  float feat[PLANNER_NF];
+  point_features<T>(dim, type, dbl, Mp, xyz, shift, scale,
+                    type == 3 ? (double)Np : (double)nmodes, tol, batchsize,
+                    std::pow(10.0, xs_product) - 1.0, feat, stream);
+  std::copy(feat, feat + PLANNER_NF, features);
+  int best = -1;
+  if (ext.planner == 2) {
+    double pred[PLANNER_K];
+    if (planner_predict(feat, pred, stream)) {
+      double best_ms = 1e300;
+      for (int k = 0; k < PLANNER_K; ++k) {
+        Candidate c;
+        if (!planner_candidate(dim, dbl, k, &c) || !candidate_valid(c)) continue;
+        if (pred[k] < best_ms) {
+          best_ms = pred[k];
+          best = k;
+        }
+      }
+    }
+  } else if (type != 3 && Mp > 0) {
+    // autotuner: time every valid candidate on a strided sample of the points,
+    // once per problem class
+    std::vector<int> key = {type, dim, (int)dbl, (int)std::lround(-4 * std::log10(tol)),
+                            (int)std::lround(2 * std::log2((double)nmodes)),
+                            (int)std::lround(4 * std::log10((double)Mp)),
+                            (int)std::lround(8 * feat[7]), (int)std::lround(10 * feat[8]),
+                            batchsize};
+    {
+      std::lock_guard<std::mutex> g(tune_mu);
+      auto it = tune_cache.find(key);
+      if (it != tune_cache.end()) best = it->second;
+    }
+    if (best < 0) {
+      const int64_t Ms = std::min<int64_t>(Mp, (int64_t)1 << 21);
+      const int64_t stride = Mp / Ms;
+      AsyncBuf sb((size_t)Ms * dim * sizeof(T), stream);
+      const T *xs[3];
+      for (int d = 0; d < dim; ++d) {
+        T *dst = sb.as<T>() + (size_t)d * Ms;
+        GBN_CUDA(cudaMemcpy2DAsync(dst, sizeof(T), xyz[d], stride * sizeof(T), sizeof(T),
+                                   (size_t)Ms, cudaMemcpyDeviceToDevice, stream));
+        xs[d] = dst;
+      }
+      for (int d = dim; d < 3; ++d) xs[d] = xs[0];
+      Mtune = Mp;
+      double best_ms = 1e300;
+      for (int k = 0; k < PLANNER_K; ++k) {
+        Candidate c;
+        if (!planner_candidate(dim, dbl, k, &c) || !candidate_valid(c)) continue;
+        const double ms_k = time_candidate(c, Ms, xs);
+        tune_ms[k] = ms_k;
+        if (ms_k < best_ms) {
+          best_ms = ms_k;
+          best = k;
+        }
+      }
+      if (best >= 0) {
+        std::lock_guard<std::mutex> g(tune_mu);
+        tune_cache[key] = best;
+      }
+    }
+  }
+  Candidate c;
+  if (best >= 0 && planner_candidate(dim, dbl, best, &c)) {
+    planned_slot = best;
+    planner_used = ext.planner;
+    return c;
+  }
+  // fallback: the reference heuristic's shape at the current sigma
+  planned_slot = -1;
+  planner_used = 1;
+  c = Candidate{opts.upsampfac, {0, 0, 0}, 1024, -1, 1};
+  return c;
+}
+
 template <typename T> PointLayout<T> Plan<T>::layout() const {
   PointLayout<T> L;
   L.dim = dim;
@@ -452,6 +659,12 @@ void Plan<T>::setpts(int64_t Mp, const T *x, const T *y, const T *z, int64_t Np,
   if (Mp > 0 && (!x || (dim > 1 && !y) || (dim > 2 && !z)))
     GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "null coordinate array");
   if (type != 3) {
+    if ((ext.planner == 2 || ext.planner == 3) && (dim == 2 || dim == 3) &&
+        !opts.gpu_spreadinterponly) {
+      const Candidate c = plan_shape(Mp, xyz, 0);
+      apply_sigma(c.sigma);
+      apply_shape(c);
+    }
     AxisMap ax[3];
     for (int d = 0; d < 3; ++d) ax[d] = AxisMap{0.0, 1.0, nf[d], bins[d]};
     sort_points(Mp, xyz, ax);
@@ -482,6 +695,13 @@ void Plan<T>::setpts(int64_t Mp, const T *x, const T *y, const T *z, int64_t Np,
       width_center(lo, hi, &t3S[d], &t3D[d]);
     }
   }
+  // planners 2/3: the upsampling factor and the outer spread's shape
+  Candidate t3c{};
+  const bool t3planned = (ext.planner == 2 || ext.planner == 3) && (dim == 2 || dim == 3);
+  if (t3planned) {
+    t3c = plan_shape(Mp, xyz, Np);
+    apply_sigma(t3c.sigma);
+  }
   int64_t nft[3] = {1, 1, 1};
   for (int d = 0; d < dim; ++d) {
     type3_grid(opts.upsampfac, t3X[d], t3S[d], K.ns, &nft[d], &t3h[d], &t3gam[d]);
@@ -499,6 +719,7 @@ void Plan<T>::setpts(int64_t Mp, const T *x, const T *y, const T *z, int64_t Np,
       printf("[gbnufft] t3 dim %d: X=%.3g C=%.3g S=%.3g D=%.3g gam=%.4g nf=%d h=%.3g\n", d,
              t3X[d], t3C[d], t3S[d], t3D[d], t3gam[d], nf[d], t3h[d]);
   choose_spread_config(opts.gpu_method != 0);
+  if (t3planned) apply_shape(t3c);
   // pre-phase exp(i isign D.x) (skipped when D = 0) and the post factor
   const bool needpre = t3D[0] != 0.0 || t3D[1] != 0.0 || t3D[2] != 0.0;
   if (needpre && Mp > 0) {
@@ -530,7 +751,9 @@ void Plan<T>::setpts(int64_t Mp, const T *x, const T *y, const T *z, int64_t Np,
   io.gpu_binsizex = io.gpu_binsizey = io.gpu_binsizez = 0;
   int64_t inner_modes[3] = {nf[0], nf[1], nf[2]};
   inner.reset();
-  inner.reset(new Plan<T>(2, dim, inner_modes, iflag, batchsize, tol, io, &ext));
+  gbnufft_opts iext = ext;
+  if (iext.planner >= 2) iext.planner = 0; // the inner type 2 takes the engine's shape
+  inner.reset(new Plan<T>(2, dim, inner_modes, iflag, batchsize, tol, io, &iext));
   AxisMap iax[3];
   for (int d = 0; d < 3; ++d)
     iax[d] = AxisMap{d < dim ? t3D[d] : 0.0, d < dim ? scale[d] : 1.0, inner->nf[d],

@@ -11,6 +11,7 @@
 #include "gbnufft_ext.h"
 #include "device_util.cuh"
 #include "elementwise.h"
+#include "planner.h"
 #include "spreadinterp.h"
 
 namespace gbn {
@@ -111,8 +112,26 @@ public:
   double t3h[3] = {1, 1, 1}, t3gam[3] = {1, 1, 1};
   std::unique_ptr<Plan<T>> inner; // type 3: the type-2 plan on the outer grid
 
+  int form = KERNEL_PSWF; // kernel form (KERNEL_ES / KERNEL_PSWF)
+  bool user_sigma = false; // the upsampling factor was given by the caller
+  int planned_slot = -1;  // planners 2/3: the candidate slot chosen at setpts
+  int planner_used = 0;   // planner whose choice is in use (2/3 fall back to 1)
+  float features[PLANNER_NF] = {}; // planners 2/3: the features of the last setpts
+  double tune_ms[PLANNER_K] = {};  // planner 3: estimated execute ms per slot (0: not timed)
+  int64_t Mtune = 0;               // points the autotuner's estimates are scaled to
+
 private:
   void choose_spread_config(bool user_method);
+  void make_kernel();
+  void make_grid();
+  void destroy_fft();
+  // planners 2 (learned) and 3 (autotuned) at setpts: pick a candidate shape;
+  // returns it (the reference heuristic's shape when the planner falls back)
+  Candidate plan_shape(int64_t M, const T *const xyz[3], int64_t N);
+  bool candidate_valid(const Candidate &c) const;
+  void apply_sigma(double sigma);      // kernel (and types 1/2: grid) at sigma
+  void apply_shape(const Candidate &c); // bins, subproblem size, variant
+  double time_candidate(const Candidate &c, int64_t Ms, const T *const xs[3]);
   void make_fft();
   void make_pruned_fft();
   void make_fseries();

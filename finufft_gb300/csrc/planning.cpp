@@ -127,18 +127,22 @@ std::vector<double> pswf0_legendre(double c) {
     if (below(mid) >= 1) hi = mid;
     else lo = mid;
   }
-  // inverse iteration on T - lo (positive definite: lo is below the eigenvalue)
+  // inverse iteration on T - sh, the shift a hair below the bracket (so below
+  // the eigenvalue whatever the rounding of the Sturm counts: T - sh is
+  // positive definite and its LDL^T pivots are positive)
+  const double sh = lo - 1e-9 * std::max(1.0, std::fabs(lo));
+  auto safe = [](double p) { return std::fabs(p) < 1e-300 ? (p < 0 ? -1e-300 : 1e-300) : p; };
   std::vector<double> v(K, 1.0), piv(K), w(K);
   for (int it = 0; it < 4; ++it) {
-    piv[0] = d[0] - lo;
+    piv[0] = safe(d[0] - sh);
     w[0] = v[0];
     for (int k = 1; k < K; ++k) {
-      const double l = e[k - 1] / std::max(piv[k - 1], 1e-300);
-      piv[k] = d[k] - lo - l * e[k - 1];
+      const double l = e[k - 1] / piv[k - 1];
+      piv[k] = safe(d[k] - sh - l * e[k - 1]);
       w[k] = v[k] - l * w[k - 1];
     }
-    v[K - 1] = w[K - 1] / std::max(piv[K - 1], 1e-300);
-    for (int k = K - 2; k >= 0; --k) v[k] = (w[k] - e[k] * v[k + 1]) / std::max(piv[k], 1e-300);
+    v[K - 1] = w[K - 1] / piv[K - 1];
+    for (int k = K - 2; k >= 0; --k) v[k] = (w[k] - e[k] * v[k + 1]) / piv[k];
     double nrm = 0;
     for (double t : v) nrm += t * t;
     nrm = std::sqrt(nrm);
@@ -258,7 +262,8 @@ KernelChoice choose_kernel(double tol, double sigma, int kerevalmeth, int is_flo
 }
 
 KernelChoice choose_kernel_pswf(double tol, double sigma, int dim, int type, int is_float,
-                                int kerformula, int spreadinterponly, int debug)
+                                int kerformula, int kerevalmeth, int spreadinterponly,
+                                int debug)
 // The CPU library's kernel (src/common/kernel.cpp:79-146): the PSWF psi_0^beta
 // with the width law ns = ceil(ln(tolfac/tol) / (pi sqrt(1 - 1/sigma)) + 1),
 // tolfac = 0.18 * 1.4^(dim-1) * (1.4 for type 3), and the shape parameter of
@@ -272,9 +277,9 @@ KernelChoice choose_kernel_pswf(double tol, double sigma, int dim, int type, int
             kerformula);
     GBN_THROW(FINUFFT_ERR_KERFORMULA_NOTVALID, "kerformula");
   }
-  // argument checks and the GPU width rule (kerevalmeth 0: any sigma is legal here,
-  // the PSWF is always evaluated from fitted pieces)
-  const KernelChoice g = choose_kernel(tol, sigma, 0, is_float, spreadinterponly, 0);
+  // argument checks (with kerevalmeth 1 the GPU interface's: Horner evaluation
+  // at sigma 2 and 1.25 only) and the GPU width rule
+  const KernelChoice g = choose_kernel(tol, sigma, kerevalmeth, is_float, spreadinterponly, 0);
   const double eps_mach = is_float ? (double)FLT_EPSILON : DBL_EPSILON;
   const double t = std::max(tol, eps_mach);
   const double tolfac = 0.18 * std::pow(1.4, dim - 1) * (type == 3 ? 1.4 : 1.0);

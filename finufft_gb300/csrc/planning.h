@@ -26,8 +26,11 @@ KernelChoice choose_kernel(double tol, double sigma, int kerevalmeth, int is_flo
 // The CPU library's kernel choice: PSWF of width max(its width law, the GPU
 // rule) and shape parameter by kerformula (0 or 8: default, 7, 9; any other
 // value throws FINUFFT_ERR_KERFORMULA_NOTVALID).
+// kerevalmeth 1 applies the GPU interface's sigma check (FINUFFT_ERR_HORNER_WRONG_BETA
+// off sigma 2 and 1.25) to a user-given sigma.
 KernelChoice choose_kernel_pswf(double tol, double sigma, int dim, int type, int is_float,
-                                int kerformula, int spreadinterponly, int debug);
+                                int kerformula, int kerevalmeth, int spreadinterponly,
+                                int debug);
 
 // ES kernel value at x (grid units), support |x| < ns/2.
 double es_kernel(double x, int ns, double beta);

@@ -20,7 +20,15 @@ extern "C" {
 typedef struct gbnufft_opts {
   int planner;        /* 0: this engine's defaults; 1: the reference library's heuristic
                          (cuFINUFFT 2.6 bin sizes, method and subproblem size,
-                         src/cuda/heuristics.cu:325-445) */
+                         src/cuda/heuristics.cu:325-445); 2: learned: at setpts a 2x64
+                         MLP predicts the execute time of each candidate shape
+                         (upsampling factor, bins, subproblem size, spread variant)
+                         from features of the points and the plan keeps the fastest
+                         candidate whose kernel reaches tol (no trained model, or
+                         features outside its training range: planner 1's shape);
+                         3: autotuned: at setpts every candidate is timed on a sample
+                         of the points (cached per problem class). 2D and 3D types
+                         1, 2, 3; 1D takes planner 0 */
   int spread_variant; /* -1 auto; tiled spread: 0 shared tile with per-point
                          atomics, 1 one warp per tile (no atomics, same-cell runs in
                          registers), 2 shared tile with same-cell register runs,
@@ -67,6 +75,10 @@ typedef struct gbnufft_plan_info {
   int maxsubprobsize;  /* points per subproblem in use */
   int spread_fixed;    /* 1: the 3D spread sums into the int32 fixed-point tile */
   int kernel_form;     /* 1 ES, 2 PSWF */
+  int planner_used;    /* planner whose shape is in use (2 and 3 fall back to 1) */
+  int planned_slot;    /* planners 2/3: candidate slot chosen at setpts (-1: none) */
+  float features[12];  /* planners 2/3: the problem's features at the last setpts */
+  double tune_ms[12];  /* planner 3: estimated execute ms per slot (0: not timed) */
 } gbnufft_plan_info;
 
 GBNUFFT_EXPORT void gbnufft_default_opts(gbnufft_opts *o);
@@ -131,6 +143,39 @@ GBNUFFT_EXPORT int gbnufft_kernel_choice(double tol, double sigma, int dim, int 
                                          double *beta);
 GBNUFFT_EXPORT int gbnufft_kernel_eval(int form, int ns, double beta, int64_t n,
                                        const double *x, double *out);
+
+/* The learned planner (no counterpart in the reference, whose heuristic is
+ * src/cuda/heuristics.cu:325-445). Sizes: features, hidden width (two hidden
+ * layers), candidate slots, weights (W1[H][NF] b1 W2[H][H] b2 W3[K][H] b3).
+ * planner_candidate: the shape of slot k for a dimension and precision
+ * (reference = 1: the reference heuristic's shape at that sigma);
+ * FINUFFT_ERR_INVALID_ARGUMENT for an unused slot. planner_model: the model
+ * compiled into the library (trained = 0: none; weights of nweights floats;
+ * feature standardisation mean/stdev and training range lo/hi of nfeat floats;
+ * output standardisation of log10 ms). planner_forward: the MLP's CUDA forward
+ * pass on device arrays x[n][nfeat] -> y[n][nslots]. planner_train: minibatch
+ * Adam on the masked squared error with the CUDA training kernels, host arrays,
+ * w updated in place, loss[epochs]. point_features: the features of a point set
+ * (device coordinates; u = (x - shift) * scale wrapped into [0,1) for the
+ * occupancy histogram). */
+GBNUFFT_EXPORT int gbnufft_planner_dims(int *nfeat, int *hidden, int *nslots, int *nweights);
+GBNUFFT_EXPORT int gbnufft_planner_candidate(int dim, int is_double, int slot, double *sigma,
+                                             int *bins, int *maxsub, int *variant,
+                                             int *reference);
+GBNUFFT_EXPORT int gbnufft_planner_model(int *trained, float *weights, float *mean,
+                                         float *stdev, float *lo, float *hi, float *ymean,
+                                         float *ystd);
+GBNUFFT_EXPORT int gbnufft_planner_forward(const float *d_weights, int n, const float *d_x,
+                                           float *d_y, void *stream);
+GBNUFFT_EXPORT int gbnufft_planner_train(int n, const float *x, const float *t,
+                                         const float *mask, int epochs, int batch, float lr,
+                                         float weight_decay, unsigned seed, float *w,
+                                         float *loss);
+GBNUFFT_EXPORT int gbnufft_point_features(int dim, int type, int is_double, int64_t M,
+                                          const void *d_x, const void *d_y, const void *d_z,
+                                          const double *shift, const double *scale,
+                                          double nmodes, double tol, int ntr,
+                                          double xs_product, float *feat, void *stream);
 
 /* Measures the device's conflict-free shared-memory f32 atomicAdd rate
  * (lane operations per second), the peak the spreading kernels are held to. */
