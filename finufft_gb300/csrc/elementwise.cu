@@ -44,6 +44,9 @@ template <typename T> size_t spread_tile2m_bytes(int ns, const int bin[3], int w
   const size_t stage = (33 * (ns + 4 * ((ns + 3) / 4) + 2) * sizeof(T) + 33 * 4 + 15) / 16 * 16;
   return tile + (size_t)warps * stage;
 }
+size_t spread_tile3x_bytes(int ns, const int bin[3], int warps) {
+  return tile3_bytes<double>(ns, bin[0], bin[1], bin[2]) + (size_t)warps * t3x_stage_bytes(ns);
+}
 template size_t spread_tile2m_bytes<float>(int, const int[3], int);
 template size_t spread_tile2m_bytes<double>(int, const int[3], int);
 template size_t spread_tile3m_bytes<float>(int, const int[3], int);

@@ -21,6 +21,8 @@ template <typename T> size_t spread_tile2m_bytes(int ns, const int bin[3], int w
 template <typename T> size_t spread_tile3v_bytes(int ns, const int bin[3], int warps);
 // Shared-memory bytes of the warp-aggregated 3D spread (variant 2).
 template <typename T> size_t spread_tile3m_bytes(int ns, const int bin[3], int warps);
+// Shared-memory bytes of the double-precision int64 fixed-point 3D spread (variant 4).
+size_t spread_tile3x_bytes(int ns, const int bin[3], int warps);
 
 // fw[t*nf + g] += sum_j c[t*M + j] (* pre[j] or conj(pre[j])) phi(g - x_j), t < ntr.
 // fw must be zeroed by the caller.

@@ -326,6 +326,227 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Method 2 in 3D, double precision: variant 4, an int64 fixed-point tile.
+// GB300 issues FP64 at a small fraction of its FP32 rate, and shared-memory
+// double atomics are compare-and-swap loops around an FP64 add, so the double
+// spread (2 ns^3 updates per point, 4394 at ns = 13) was bound by FP64 issue.
+// Here each block first sums S = sum_j (|Re c_j| + |Im c_j|) over its
+// subproblem; a tile cell's sum is at most S (kernel values are at most 1;
+// margin 1.01), so the tile holds round(value * 2^e) in int64 with the power
+// of two 2^e <= 2^62 / (1.01 S), added by native 64-bit integer atomics. The
+// per-cell products are formed in double-float arithmetic (hi + lo float
+// pairs, ~46 significant bits, fused multiply-adds on the FP32 pipe) from the
+// FP64 kernel weights and strengths staged per point, and converted to int64
+// as round(hi) + round(lo). The integer sums are exact; each contribution is
+// rounded to S 2^-62 and carries the float pair's relative error (~2^-45),
+// far below the double-precision tolerances (the kernel is used at ns >= 6).
+// Subproblems whose S is not finite, or so small that 2^e would overflow,
+// sum doubles in the same tile with compare-and-swap atomics instead.
+// Staging and lane mapping follow spread_tile3_kernel.
+struct dfloat {
+  float h, l;
+};
+__device__ __forceinline__ dfloat df_from(double a) {
+  const float h = __double2float_rn(a);
+  return {h, __double2float_rn(a - (double)h)};
+}
+__device__ __forceinline__ dfloat df_mul(dfloat a, dfloat b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p); // the product's rounding error, exactly
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float h = p + e;
+  return {h, e - (h - p)};
+}
+__device__ __forceinline__ long long df_to_ll(dfloat a) {
+  return __float2ll_rn(a.h) + __float2ll_rn(a.l);
+}
+
+template <int NS>
+__global__ void __launch_bounds__(256)
+    spread_tile3x_kernel(PointLayout<double> L0, KernelShape<double> K,
+                         const double2 *__restrict__ c, const double2 *__restrict__ pre,
+                         int conj_pre, double2 *__restrict__ fw, int64_t nf_total) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[8];
+  __shared__ int mode; // 0: fixed point, 1: double atomics
+  __shared__ double inv_scale;
+  __shared__ float scale_f;
+  constexpr int SK = STAGE_STRIDE;
+  constexpr int NXB = (NS + 7) / 8;
+  constexpr int NPAIR = NS * NS;
+  constexpr int NROUND = (NPAIR + 3) / 4;
+  const int sub = blockIdx.x;
+  const int tr = blockIdx.y;
+  int b = L0.sub_bin[sub];
+  PointLayout<double> Lg;
+  const int64_t goff = resolve_problem<double>(L0, Lg, b);
+  const PointLayout<double> &L = Lg;
+  const int p0 = L.sub_start[sub];
+  const int np = L.sub_count[sub];
+  const TileGeom<3> G = tile_of<double, 3, NS>(L, b);
+  const int px = tile_pitch_x(3, G.t[0]);
+  const int py = tile3_py(G.t[1], NS);
+  const int Q = px * py;
+  const int ncell = Q * G.t[2];
+  long long *ire = reinterpret_cast<long long *>(smem_raw);
+  long long *iim = ire + ncell;
+  double *dre = reinterpret_cast<double *>(ire), *dim_ = reinterpret_cast<double *>(iim);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  unsigned char *stage = smem_raw + tile3_bytes<double>(NS, L.bin[0], L.bin[1], L.bin[2]) +
+                         (size_t)warp * t3x_stage_bytes(NS);
+  float *kxh = reinterpret_cast<float *>(stage);
+  float *kxl = kxh + NS * SK;
+  float *kyh = kxl + NS * SK;
+  float *kyl = kyh + NS * SK;
+  float *kzh = kyl + NS * SK;
+  float *kzl = kzh + NS * SK;
+  float *vrh = kzl + NS * SK;
+  float *vrl = vrh + SK;
+  float *vih = vrl + SK;
+  float *vil = vih + SK;
+  int *spk = reinterpret_cast<int *>(vil + SK);
+  const double2 *ct = c + (int64_t)tr * L.M;
+  // the subproblem's strength sum S, and the tile's scale
+  double part = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    const int j = L.perm[p0 + i];
+    double2 v = ct[j];
+    if (pre) v = cmul_opt<double>(v, pre[j], conj_pre);
+    part += fabs(v.x) + fabs(v.y);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if (lane == 0) red[warp] = part;
+  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+    ire[i] = 0;
+    iim[i] = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double S = 0.0;
+    for (int w = 0; w < nwarp; ++w) S += red[w];
+    int e = 0;
+    mode = 0;
+    if (!(S < 1e300)) {
+      mode = 1; // inf or NaN strengths: keep IEEE propagation
+    } else if (S > 0.0) {
+      e = 62 - (int)ceil(log2(1.01 * S));
+      // 2^e must be a normal float, as must the staged scaled strengths
+      if (e > 120 || e < -126) mode = 1;
+    }
+    scale_f = mode ? 1.0f : __int_as_float((e + 127) << 23); // 2^e
+    inv_scale = mode ? 1.0 : ldexp(1.0, -e);
+  }
+  __syncthreads();
+  const bool fx = mode == 0;
+  const double sc = fx ? (double)scale_f : 1.0;
+  const int lx = lane & 7, lp = lane >> 3;
+  for (int base = warp * 32; base < np; base += nwarp * 32) {
+    const int i = base + lane;
+    if (i < np) {
+      const int p = p0 + i;
+      const int j = L.perm[p];
+      double2 v = ct[j];
+      if (pre) v = cmul_opt<double>(v, pre[j], conj_pre);
+      double kk[NS];
+      const int sx = point_weights<double, NS>(L.loc[0][p], L.bin[0], K, kk);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) {
+        const dfloat d = df_from(kk[a]);
+        kxh[a * SK + lane] = d.h;
+        kxl[a * SK + lane] = d.l;
+      }
+      const int sy = point_weights<double, NS>(L.loc[1][p], L.bin[1], K, kk);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) {
+        const dfloat d = df_from(kk[a]);
+        kyh[a * SK + lane] = d.h;
+        kyl[a * SK + lane] = d.l;
+      }
+      const int sz = point_weights<double, NS>(L.loc[2][p], L.bin[2], K, kk);
+#pragma unroll
+      for (int a = 0; a < NS; ++a) {
+        const dfloat d = df_from(kk[a]);
+        kzh[a * SK + lane] = d.h;
+        kzl[a * SK + lane] = d.l;
+      }
+      const dfloat vr = df_from(v.x * sc), vi = df_from(v.y * sc);
+      vrh[lane] = vr.h;
+      vrl[lane] = vr.l;
+      vih[lane] = vi.h;
+      vil[lane] = vi.l;
+      spk[lane] = sx | (sy << 10) | (sz << 20);
+    }
+    __syncwarp();
+    const int cnt = min(32, np - base);
+    for (int q = 0; q < cnt; ++q) {
+      const int sp = spk[q];
+      const int rowbase = (sp >> 20) * Q + ((sp >> 10) & 1023) * px + (sp & 1023);
+      const dfloat vr = {vrh[q], vrl[q]}, vi = {vih[q], vil[q]};
+      dfloat ar[NXB], ai[NXB];
+#pragma unroll
+      for (int xb = 0; xb < NXB; ++xb) {
+        const int dx = min(xb * 8 + lx, NS - 1);
+        const dfloat wx = {kxh[dx * SK + q], kxl[dx * SK + q]};
+        ar[xb] = df_mul(vr, wx);
+        ai[xb] = df_mul(vi, wx);
+      }
+#pragma unroll 4
+      for (int r = 0; r < NROUND; ++r) {
+        const int pp = 4 * r + lp;
+        if (pp < NPAIR) {
+          const int dy = pp % NS, dz = pp / NS;
+          const dfloat wyz = df_mul({kyh[dy * SK + q], kyl[dy * SK + q]},
+                                    {kzh[dz * SK + q], kzl[dz * SK + q]});
+          const int a0 = rowbase + dz * Q + dy * px + lx;
+#pragma unroll
+          for (int xb = 0; xb < NXB; ++xb) {
+            if (xb * 8 + lx < NS) {
+              const dfloat tr_ = df_mul(ar[xb], wyz), ti = df_mul(ai[xb], wyz);
+              const int a = a0 + xb * 8;
+              if (fx) {
+                atomicAdd(reinterpret_cast<unsigned long long *>(ire + a),
+                          (unsigned long long)df_to_ll(tr_));
+                atomicAdd(reinterpret_cast<unsigned long long *>(iim + a),
+                          (unsigned long long)df_to_ll(ti));
+              } else {
+                atomicAdd(dre + a, (double)tr_.h + (double)tr_.l);
+                atomicAdd(dim_ + a, (double)ti.h + (double)ti.l);
+              }
+            }
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  double2 *fwt = fw + (int64_t)tr * nf_total + goff;
+  const double is = inv_scale;
+  for (int q = threadIdx.x; q < G.cells; q += blockDim.x) {
+    const int x = q % G.t[0];
+    const int y = (q / G.t[0]) % G.t[1];
+    const int z = q / (G.t[0] * G.t[1]);
+    const int sidx = z * Q + y * px + x;
+    double2 v;
+    if (fx) {
+      const long long a = ire[sidx], bb = iim[sidx];
+      if ((a | bb) == 0) continue;
+      v.x = (double)a * is;
+      v.y = (double)bb * is;
+    } else {
+      v.x = dre[sidx];
+      v.y = dim_[sidx];
+    }
+    const int64_t g = wrap_idx(G.org[0] + x, L.nf[0]) +
+                      (int64_t)L.nf[0] * (wrap_idx(G.org[1] + y, L.nf[1]) +
+                                          (int64_t)L.nf[1] * wrap_idx(G.org[2] + z, L.nf[2]));
+    atomic_add_cplx_global(fwt + g, v);
+  }
+}
+
 // threads of the warp-aggregated 3D spread: 12 warps share a tile in single
 // precision, 8 in double (twice the accumulator registers); 2 blocks per SM
 template <typename T> __host__ __device__ constexpr int t3m_threads() {
@@ -1577,6 +1798,16 @@ template <typename T, int DIM> struct Dispatch {
         km<<<grid, t3m_threads<T>(), cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
         GBN_LAUNCH_CHECK();
         return;
+      }
+      if constexpr (sizeof(T) == 8) {
+        if (cfg.variant == 4) {
+          auto kx = spread_tile3x_kernel<NS>;
+          GBN_CUDA(cudaFuncSetAttribute(kx, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)cfg.smem));
+          kx<<<grid, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
+          GBN_LAUNCH_CHECK();
+          return;
+        }
       }
       if (cfg.variant == 1) {
         auto kw = spread_tile3w_kernel<T, NS>;

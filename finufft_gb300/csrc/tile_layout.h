@@ -77,4 +77,11 @@ __host__ __device__ constexpr size_t tile3v_bytes(int ns, int bx, int by, int bz
           15) / 16 * 16;
 }
 
+// Double-precision 3D spread into an int64 fixed-point tile (variant 4):
+// per-warp staging of 32 points as float pairs (hi, lo) -- x, y and z weights,
+// the two strength components -- and packed start cells.
+__host__ __device__ constexpr int t3x_stage_bytes(int ns) {
+  return (STAGE_STRIDE * (6 * ns + 4) * 4 + STAGE_STRIDE * 4 + 15) / 16 * 16;
+}
+
 } // namespace gbn

@@ -411,3 +411,47 @@ def test_spread_variants_2d(oracle, dtype, tol):
         assert oracle.rel_l2(outs[v][1].ravel(), ref) < bound, v
         if v:
             assert oracle.rel_l2(outs[v], outs[0]) < (2e-5 if dtype == "complex64" else 1e-12), v
+
+
+@pytest.mark.parametrize("tol", [1e-7, 1e-9, 1e-12, 1e-14])
+@pytest.mark.parametrize("scale", [1.0, 1e20, 1e200, 1e-200])
+def test_fp64_fixed_point_tile(oracle, tol, scale):
+    """double-precision 3D spread with the int64 fixed-point tile (variant 4,
+    the default for widths above 5) against the double-atomic tile (variant 0)
+    and the FP64 direct sum, on clustered points at strength scales where the
+    tile's power-of-two scale is used (1, 1e20) and where a subproblem falls
+    back to double atomics (1e200, 1e-200)"""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(104)
+    nm, M = (14, 16, 12), 6000
+    pts = _clustered(rng, 3, M, np.float64)
+    c = _cx(rng, M, "complex128") * scale
+    c[:40] *= 500.0  # strong sources among weak ones
+    outs = {}
+    for v in (-1, 0):
+        plan = fg.Plan(1, nm, eps=tol, dtype="complex128", isign=1, spread_variant=v)
+        outs[v, "used"] = plan.info().spread_variant
+        plan.setpts(*[_dev(p) for p in pts])
+        outs[v] = plan.execute(_dev(c)).cpu().numpy().ravel() / scale
+    assert outs[-1, "used"] == (4 if plan.info().ns > 5 else 3)
+    assert outs[0, "used"] == 0
+    assert oracle.rel_l2(outs[-1], outs[0]) < 1e-13
+    ref = oracle.dirft1(_oracle_pts(pts), c / scale, 1, nm[::-1])
+    same = oracle.nufft_es(1, _oracle_pts(pts), c / scale, 1, tol, n_modes=nm[::-1],
+                           is_float=False, kernel=_kernel(plan))
+    assert oracle.rel_l2(outs[-1], ref) < _bound(oracle.rel_l2(same, ref), "complex128")
+
+
+def test_fp64_fixed_point_tile_nan():
+    """a NaN strength reaches the output (its subproblem sums doubles)"""
+    import finufft_gb300 as fg
+
+    rng = np.random.default_rng(105)
+    pts = _clustered(rng, 3, 3000, np.float64)
+    c = _cx(rng, 3000, "complex128")
+    c[7] = np.nan
+    plan = fg.Plan(1, (12, 12, 12), eps=1e-12, dtype="complex128", isign=1)
+    assert plan.info().spread_variant == 4
+    plan.setpts(*[_dev(p) for p in pts])
+    assert np.isnan(plan.execute(_dev(c)).cpu().numpy()).any()
