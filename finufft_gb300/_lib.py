@@ -162,6 +162,8 @@ def _declare(lib):
     lib.gbnufft_kernel_choice.restype = c_int
     lib.gbnufft_kernel_eval.argtypes = [c_int, c_int, c_double, c_int64, c_void_p, c_void_p]
     lib.gbnufft_kernel_eval.restype = c_int
+    lib.gbnufft_device_error.argtypes = [c_int, POINTER(c_int)]
+    lib.gbnufft_device_error.restype = c_int
     ip = POINTER(c_int)
     fp = POINTER(c_float)
     lib.gbnufft_planner_dims.argtypes = [ip, ip, ip, ip]

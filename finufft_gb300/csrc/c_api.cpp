@@ -411,6 +411,14 @@ int gbnufft_point_features(int dim, int type, int is_double, int64_t M, const vo
   });
 }
 
+int gbnufft_device_error(int device, int *code) {
+  return guarded([&] {
+    if (!code) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "code");
+    gbn::DeviceScope ds(device);
+    *code = gbn::device_error_take();
+  });
+}
+
 int gbnufft_smem_atomic_rate(int device, double *rate) {
   return guarded([&] {
     if (!rate) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "rate");

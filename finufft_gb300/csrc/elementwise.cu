@@ -1,3 +1,5 @@
+#include <map>
+#include <mutex>
 // Deconvolution / amplification, kernel Fourier series and type-3 phase
 // kernels, plus the host dispatch of the spread/interp translation units.
 #include <vector>
@@ -55,6 +57,31 @@ template size_t spread_tile3w_bytes<float>(int, const int[3]);
 template size_t spread_tile3w_bytes<double>(int, const int[3]);
 template size_t spread_tile_smem<float>(int, int, const int[3], int);
 template size_t spread_tile_smem<double>(int, int, const int[3], int);
+
+namespace {
+std::mutex err_mu;
+std::map<int, int *> err_words;
+} // namespace
+
+int *device_error_word() {
+  int dev = 0;
+  GBN_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> g(err_mu);
+  int *&w = err_words[dev];
+  if (!w) {
+    GBN_CUDA(cudaMalloc((void **)&w, sizeof(int)));
+    GBN_CUDA(cudaMemset(w, 0, sizeof(int)));
+  }
+  return w;
+}
+
+int device_error_take() {
+  int *w = device_error_word();
+  int v = 0;
+  GBN_CUDA(cudaMemcpy(&v, w, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) GBN_CUDA(cudaMemset(w, 0, sizeof(int)));
+  return v;
+}
 
 template <typename T>
 void launch_spread(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *c,

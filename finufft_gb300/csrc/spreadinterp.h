@@ -24,6 +24,11 @@ template <typename T> size_t spread_tile3m_bytes(int ns, const int bin[3], int w
 // Shared-memory bytes of the double-precision int64 fixed-point 3D spread (variant 4).
 size_t spread_tile3x_bytes(int ns, const int bin[3], int warps);
 
+// A device word (one per device, allocated at first use) where kernels whose
+// bounded waits give up record it; device_error_take reads and clears it.
+int *device_error_word();
+int device_error_take();
+
 // fw[t*nf + g] += sum_j c[t*M + j] (* pre[j] or conj(pre[j])) phi(g - x_j), t < ntr.
 // fw must be zeroed by the caller.
 template <typename T>

@@ -8,6 +8,8 @@
 // support cell in tile coordinates is s = ceil(l - ns/2) + floor(ns/2) in
 // [0, bin] and its kernel weights are phi(ceil(l - ns/2) - l + j), j < ns.
 #pragma once
+#include <cuda.h>
+
 #include <algorithm>
 #include <cstdlib>
 #include "device_util.cuh"
@@ -1758,6 +1760,8 @@ __global__ void __launch_bounds__(INTERP_TILE_THREADS)
   }
 }
 
+#include "interp_tma.cuh"
+
 // out[t*M + perm[p]] = src[t*M + p]: sorted-order interpolation results to user
 // order, transform by transform (blockIdx.y), so that the 8-byte scattered
 // writes of one transform combine into full sectors in L2
@@ -1771,6 +1775,57 @@ __global__ void __launch_bounds__(256)
 }
 
 // ------------------------------------------------------------- dispatch ----
+// Tensor map of the fine grids for the TMA interpolation: rank dim + 1
+// (x, y, [z], transform), 8-byte elements (x counted in doubles for double
+// precision), box (BX, BY, BZ, 1). False when the driver rejects it.
+template <typename T>
+bool encode_grid_map(CUtensorMap *map, const void *base, int dim, const int nf[3], int ntr,
+                     int BX, int BY, int BZ) {
+  using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                              const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                              const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static Encode fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &f, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    cudaGetLastError();
+    return reinterpret_cast<Encode>(f);
+  }();
+  if (!fn || (reinterpret_cast<uintptr_t>(base) & 15)) return false;
+  const int xm = sizeof(T) == 8 ? 2 : 1;
+  const int rank = dim + 1;
+  const cuuint64_t esz = 8;
+  cuuint64_t gdim[4], gstr[3];
+  cuuint32_t box[4], estr[4] = {1, 1, 1, 1};
+  gdim[0] = (cuuint64_t)nf[0] * xm;
+  gdim[1] = (cuuint64_t)nf[1];
+  box[0] = (cuuint32_t)(BX * xm);
+  box[1] = (cuuint32_t)BY;
+  gstr[0] = (cuuint64_t)nf[0] * xm * esz;
+  if (dim == 2) {
+    gdim[2] = (cuuint64_t)ntr;
+    box[2] = 1;
+    gstr[1] = gstr[0] * nf[1];
+  } else {
+    gdim[2] = (cuuint64_t)nf[2];
+    gdim[3] = (cuuint64_t)ntr;
+    box[2] = (cuuint32_t)BZ;
+    box[3] = 1;
+    gstr[1] = gstr[0] * nf[1];
+    gstr[2] = gstr[1] * nf[2];
+  }
+  const CUtensorMapDataType ty =
+      sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_INT64;
+  const CUresult r = fn(map, ty, (cuuint32_t)rank, const_cast<void *>(base), gdim, gstr, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 template <typename T, int DIM> struct Dispatch {
   template <int NS>
   static void spread(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<T> *c,
@@ -1844,6 +1899,33 @@ template <typename T, int DIM> struct Dispatch {
                      int64_t nf_total, const cplx<T> *post, int conj_post, cplx<T> *out,
                      int ntr, cudaStream_t s) {
     if constexpr (DIM >= 2) {
+      // TMA-staged tiles (interp_mode 0 or 3) for single problems whose boxes fit
+      // the copy engine's limits and two buffers fit beside another block
+      if (!L.probs && (L.interp_mode == 0 || L.interp_mode == 3) && L.M > 0) {
+        const int t0 = L.bin[0] + NS, t1 = L.bin[1] + NS, t2 = DIM == 3 ? L.bin[2] + NS : 1;
+        const int BX = (t0 + 2) & ~1; // even, at least t0 + 1
+        const int xm = sizeof(T) == 8 ? 2 : 1;
+        const size_t box = (size_t)BX * t1 * t2 * sizeof(cplx<T>);
+        const size_t smem = 2 * ((box + 127) / 128 * 128);
+        CUtensorMap map;
+        if (BX * xm <= 256 && t1 <= 256 && t2 <= 256 && BX <= L.nf[0] && smem <= 100 * 1024 &&
+            encode_grid_map<T>(&map, fw, DIM, L.nf, ntr, BX, t1, t2)) {
+          auto kt = interp_tma_kernel<T, DIM, NS>;
+          GBN_CUDA(cudaFuncSetAttribute(kt, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+          kt<<<(unsigned)L.nsub, INTERP_TMA_THREADS, smem, s>>>(
+              map, L, K, fw, nf_total, post, conj_post, out, ntr, BX, t1, t2,
+              device_error_word());
+          GBN_LAUNCH_CHECK();
+          if (L.sorted_out) {
+            const unsigned gx = (unsigned)std::min<int64_t>((L.M + 255) / 256, 152 * 8);
+            scatter_sorted_kernel<T><<<dim3(gx, (unsigned)ntr), 256, 0, s>>>(
+                static_cast<const cplx<T> *>(L.sorted_out), L.perm, L.M, out);
+            GBN_LAUNCH_CHECK();
+          }
+          return;
+        }
+      }
       // tile-staged interpolation when one transform's tile fits the per-block
       // budget (three blocks per SM); interp_mode 1 keeps the gather
       const int imethod = L.interp_mode == 1 ? 0 : 1;

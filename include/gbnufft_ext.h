@@ -52,9 +52,13 @@ typedef struct gbnufft_opts {
                          0 or 8 (default), 7, 9; other values are rejected */
   int sort_keys;      /* 0 (default): points sorted by bin and, inside the bin, by the
                          first cell of their kernel support; 1: by bin and cell */
-  int interp_mode;    /* type 2 interpolation: 0 auto; 1 one thread per point gathering
-                         from the grid; 2 shared-memory tiles writing user order directly
-                         (auto may write sorted order and scatter it per transform) */
+  int interp_mode;    /* type 2 interpolation: 0 auto (3 where its boxes fit, else 2, and
+                         batches may write sorted order and scatter it per transform);
+                         1 one thread per point gathering from the grid; 2 tiles loaded
+                         into shared memory by the block's threads, user order written
+                         directly; 3 tiles copied by the tensor memory accelerator
+                         (bulk tensor copies, two buffers: the next transform's tile
+                         loads while the current one is interpolated) */
   int reserved[8];
 } gbnufft_opts;
 
@@ -176,6 +180,11 @@ GBNUFFT_EXPORT int gbnufft_point_features(int dim, int type, int is_double, int6
                                           const double *shift, const double *scale,
                                           double nmodes, double tol, int ntr,
                                           double xs_product, float *feat, void *stream);
+
+/* Reads and clears the device's error word: nonzero when a kernel's bounded
+ * wait gave up (a bulk tensor copy of the interpolation tiles that did not
+ * complete); that launch's outputs are then incomplete. 0 or a FINUFFT_ERR_*. */
+GBNUFFT_EXPORT int gbnufft_device_error(int device, int *code);
 
 /* Measures the device's conflict-free shared-memory f32 atomicAdd rate
  * (lane operations per second), the peak the spreading kernels are held to. */

@@ -455,3 +455,43 @@ def test_fp64_fixed_point_tile_nan():
     assert plan.info().spread_variant == 4
     plan.setpts(*[_dev(p) for p in pts])
     assert np.isnan(plan.execute(_dev(c)).cpu().numpy()).any()
+
+
+@pytest.mark.parametrize("dim,dtype", [(2, "complex64"), (3, "complex64"), (2, "complex128"),
+                                       (3, "complex128")])
+@pytest.mark.parametrize("ntr", [1, 3, 8])
+def test_interp_modes_agree(oracle, dim, dtype, ntr):
+    """type 2 through the three interpolation schedules -- per-point gather (1),
+    block-loaded tiles (2) and TMA-copied tiles with two buffers (3) -- on
+    clustered points with subproblems larger than one pass of the block
+    (maxsub 4096) and tiles on the periodic boundary: the same values to
+    rounding, and the FP64 direct sum within the bar; no bounded wait gave up"""
+    import ctypes
+
+    import finufft_gb300 as fg
+
+    rdt = np.float32 if dtype == "complex64" else np.float64
+    tol = 1e-5 if dtype == "complex64" else 1e-11
+    rng = np.random.default_rng(120 + dim + ntr)
+    nm = (60, 52) if dim == 2 else (20, 18, 22)
+    M = 30000
+    pts = _clustered(rng, dim, M, rdt)
+    pts[:, :200] = rdt(np.pi) - rdt(1e-3) * rng.random((dim, 200)).astype(rdt)  # seam tiles
+    fk = _cx(rng, (ntr,) + nm, dtype)
+    outs = {}
+    for mode in (1, 2, 3):
+        plan = fg.Plan(2, nm, n_trans=ntr, eps=tol, dtype=dtype, isign=-1, interp_mode=mode,
+                       gpu_maxsubprobsize=4096, gpu_maxbatchsize=ntr)
+        plan.setpts(*[_dev(p) for p in pts])
+        outs[mode] = plan.execute(_dev(fk)).cpu().numpy().reshape(ntr, M)
+    lib = fg.load_library()
+    code = ctypes.c_int(-1)
+    assert lib.gbnufft_device_error(0, ctypes.byref(code)) == 0 and code.value == 0
+    agree = 2e-6 if dtype == "complex64" else 1e-13
+    assert oracle.rel_l2(outs[3], outs[1]) < agree
+    assert oracle.rel_l2(outs[2], outs[1]) < agree
+    k = ntr - 1
+    ref = oracle.dirft2(_oracle_pts(pts), fk[k].ravel(), -1, nm[::-1])
+    same = oracle.nufft_es(2, _oracle_pts(pts), fk[k], -1, tol, n_modes=nm[::-1],
+                           is_float=dtype == "complex64", kernel=_kernel(plan))
+    assert oracle.rel_l2(outs[3][k], ref) < _bound(oracle.rel_l2(same, ref), dtype)
