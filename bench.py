@@ -285,8 +285,7 @@ def run_gpu(args):
     plan_kw = {}
     if args.variant >= 0:
         plan_kw["spread_variant"] = args.variant
-    if args.planner:
-        plan_kw["planner"] = args.planner
+    plan_kw["planner"] = args.planner
     if args.bins:
         bx, by, bz = (int(v) for v in args.bins.split(","))
         plan_kw.update(gpu_binsizex=bx, gpu_binsizey=by, gpu_binsizez=bz)
@@ -324,14 +323,16 @@ def run_gpu(args):
 
     # plain GPU form: one transform, the reference library's heuristic planning
     plain_kw = dict(plan_kw)
-    plain_kw.setdefault("planner", 1)
+    plain_kw["planner"] = 1
     ms_plain, st_plain, info_plain, _, f_plain = single(plain_kw)
     if args.only == "plain":
         print(json.dumps({"plain_ms": ms_plain, "stage_ms": st_plain, "M": M,
                           "nsub": info_plain.nsub, "bins": list(info_plain.bins)}))
         return
-    # this engine's planning, one transform
-    ms_eng, st_eng, info_eng, setpts_s, f_eng = single(plan_kw)
+    # this engine's fixed default planning (planner 0), one transform
+    eng_kw = dict(plan_kw)
+    eng_kw["planner"] = 0
+    ms_eng, st_eng, info_eng, setpts_s, f_eng = single(eng_kw)
     if args.only == "engine":
         print(json.dumps({"engine_ms": ms_eng, "stage_ms": st_eng, "M": M,
                           "nsub": info_eng.nsub, "bins": list(info_eng.bins)}))
@@ -453,7 +454,12 @@ def run_gpu(args):
         "config": {"workload": WORKLOAD, "ntransf_batched": nt, "M": M, "N": list(N_MODES),
                    "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas",
                    "ns": ns, "nf": list(binfo.nf), "bins": list(binfo.bins),
-                   "nsub": binfo.nsub, "kernel": "PSWF" if binfo.kernel_form == 2 else "ES"},
+                   "nsub": binfo.nsub, "kernel": "PSWF" if binfo.kernel_form == 2 else "ES",
+                   "planner": {0: "engine default", 1: "reference heuristic", 2: "learned",
+                               3: "autotuned"}.get(args.planner),
+                   "planner_used": binfo.planner_used, "planned_slot": binfo.planned_slot,
+                   "upsampfac": binfo.upsampfac, "spread_variant": binfo.spread_variant,
+                   "maxsubprobsize": binfo.maxsubprobsize},
         "plain": {"value": job_value(M, world, ms_plain), "ms_per_step": ms_plain,
                   "planner": "reference heuristic (cuFINUFFT 2.6: ES kernel, method 2, "
                              "bins from the shared-memory budget, 1024-point subproblems)",
@@ -564,7 +570,7 @@ def cfg_c2(args, dev, stream, with_cpu=True):
     ms_plain, c_plain = single({"planner": 1})
     ms1, c1 = single({})
     pb = fg.Plan(2, N, n_trans=nt, eps=tol, isign=-1, gpu_stream=stream.cuda_stream,
-                 gpu_maxbatchsize=nt)
+                 gpu_maxbatchsize=nt, planner=args.planner)
     pb.setpts(x, y)
     cb = torch.empty(nt, M, dtype=torch.complex64, device=dev)
     pb.execute(fk, out=cb)
@@ -716,7 +722,8 @@ def cfg_c5(args, dev, stream, with_cpu=True):
     ss = ((torch.rand(3, K, generator=g, device="cuda", dtype=torch.float64) * 2 - 1) * ht).to(torch.float32)
     c = torch.randn(M, 2, generator=g, device="cuda").view(torch.complex64)[:, 0]
     res = {}
-    for name, kw in (("plain", {"planner": 1}), ("engine", {})):
+    for name, kw in (("plain", {"planner": 1}), ("engine", {"planner": 0}),
+                     ("planned", {"planner": args.planner})):
         p = fg.Plan(3, 3, eps=tol, gpu_stream=stream.cuda_stream, **kw)
         p.setpts(xs[0], xs[1], xs[2], s=ss[0], t=ss[1], u=ss[2])
         f = torch.empty(K, dtype=torch.complex64, device=dev)
@@ -725,12 +732,18 @@ def cfg_c5(args, dev, stream, with_cpu=True):
         del p
     sel = torch.as_tensor(np.random.default_rng(17).choice(K, 10000, replace=False), device=dev)
     ref = direct_type3([xs[0], xs[1], xs[2]], c, [ss[0][sel], ss[1][sel], ss[2][sel]], +1, dev)
-    ms, f, info = res["engine"]
+    ms, f, info = res["planned"]
     out = {"workload": "3D type 3 FP32, M=K=1e7, boxes (1,2,4) x (200,100,50), tol 1e-6",
            "value": (M + K) / (ms * 1e-3), "unit": "NU pts/s (M+K)", "ms_per_step": ms,
+           "planner": args.planner, "planner_used": info.planner_used,
+           "planned_slot": info.planned_slot,
            "plain": {"value": (M + K) / (res["plain"][0] * 1e-3), "ms_per_step": res["plain"][0],
                      "planner": "reference heuristic",
                      "rel_l2": rel_l2(res["plain"][1][sel], ref)},
+           "engine_default": {"value": (M + K) / (res["engine"][0] * 1e-3),
+                              "ms_per_step": res["engine"][0],
+                              "upsampfac": res["engine"][2].upsampfac,
+                              "rel_l2": rel_l2(res["engine"][1][sel], ref)},
            "upsampfac": info.upsampfac, "ns": info.ns, "nf": list(info.nf),
            "inner_nf": list(info.inner_nf)}
     gerr = rel_l2(f[sel], ref)
@@ -900,7 +913,8 @@ def main():
     ap.add_argument("--bins", default="", help="bin sizes x,y,z (default: the planner's)")
     ap.add_argument("--maxsub", type=int, default=0, help="max points per subproblem")
     ap.add_argument("--variant", type=int, default=-1, help="3D spread variant (tuning runs)")
-    ap.add_argument("--planner", type=int, default=0, help="planner of the engine's forms")
+    ap.add_argument("--planner", type=int, default=2,
+                    help="planner of the planned forms (2 learned, 3 autotuned, 0 fixed default)")
     ap.add_argument("--only", default="", choices=["", "plain", "engine"],
                     help="time only the single-transform plan of that form (profiling runs)")
     args = ap.parse_args()

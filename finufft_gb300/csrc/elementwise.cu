@@ -1,3 +1,4 @@
+#include <limits>
 #include <map>
 #include <mutex>
 // Deconvolution / amplification, kernel Fourier series and type-3 phase
@@ -46,6 +47,14 @@ template <typename T> size_t spread_tile2m_bytes(int ns, const int bin[3], int w
   const size_t stage = (33 * (ns + 4 * ((ns + 3) / 4) + 2) * sizeof(T) + 33 * 4 + 15) / 16 * 16;
   return tile + (size_t)warps * stage;
 }
+template <typename T> size_t spread_output_driven_bytes(int dim, int ns, const int bin[3]) {
+  size_t cells = 1;
+  for (int d = 0; d < dim; ++d) cells *= (size_t)(bin[d] + ns);
+  return 2 * sizeof(T) * cells + 64 * ((size_t)dim * ns * sizeof(T) + 2 * sizeof(T) + dim * 4);
+}
+template size_t spread_output_driven_bytes<float>(int, int, const int[3]);
+template size_t spread_output_driven_bytes<double>(int, int, const int[3]);
+
 size_t spread_tile3x_bytes(int ns, const int bin[3], int warps) {
   return tile3_bytes<double>(ns, bin[0], bin[1], bin[2]) + (size_t)warps * t3x_stage_bytes(ns);
 }
@@ -140,85 +149,109 @@ __global__ void inv_fseries_kernel(int nf, QuadNodes Q, T *inv) {
   }
 }
 
+// Deconvolution and amplification walk rows along x: one block per chunk of
+// DC_X positions of one row (a row = fixed y, z and transform), so the row's
+// indices, its y/z factors and its grid row are found once per block with
+// 32-bit arithmetic, and the threads read and write contiguous x runs.
+constexpr int DC_THREADS = 256;
+constexpr int DC_X = 1024; // x positions per block
+
+// fk[t][k] = fw[t][wrap(k)] / (phihat_x(kx) phihat_y(ky) phihat_z(kz)) (type 1)
 template <typename T, int DIM>
-__global__ void deconv_kernel(int ms0, int ms1, int ms2, int nf0, int nf1, int nf2, int modeord,
-                              const T *__restrict__ i0, const T *__restrict__ i1,
-                              const T *__restrict__ i2, const cplx<T> *__restrict__ fw,
-                              int64_t nf_total, cplx<T> *__restrict__ fk, int64_t nmodes, int ntr) {
-  const int64_t total = nmodes * ntr;
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
-       q += (int64_t)gridDim.x * blockDim.x) {
-    const int tr = (int)(q / nmodes);
-    const int64_t i = q - (int64_t)tr * nmodes;
-    const int ix = (int)(i % ms0);
+__global__ void __launch_bounds__(DC_THREADS)
+    deconv_kernel(int ms0, int ms1, int ms2, int nf0, int nf1, int nf2, int modeord,
+                  const T *__restrict__ i0, const T *__restrict__ i1, const T *__restrict__ i2,
+                  const cplx<T> *__restrict__ fw, int64_t nf_total, cplx<T> *__restrict__ fk,
+                  int64_t nmodes, int xchunks) {
+  const int row = blockIdx.x / xchunks;
+  const int x0 = (blockIdx.x - row * xchunks) * DC_X;
+  int iy = 0, iz = 0, tr = row;
+  if (DIM > 1) {
+    iy = row % ms1;
+    tr = row / ms1;
+  }
+  if (DIM > 2) {
+    iz = tr % ms2;
+    tr /= ms2;
+  }
+  T fyz = T(1);
+  int64_t grow = (int64_t)tr * nf_total;
+  if (DIM > 1) {
+    const int ky = mode_of(iy, ms1, modeord);
+    grow += (int64_t)nf0 * (ky >= 0 ? ky : nf1 + ky);
+    fyz = i1[ky >= 0 ? ky : -ky];
+  }
+  if (DIM > 2) {
+    const int kz = mode_of(iz, ms2, modeord);
+    grow += (int64_t)nf0 * nf1 * (kz >= 0 ? kz : nf2 + kz);
+    fyz *= i2[kz >= 0 ? kz : -kz];
+  }
+  const int64_t orow = (int64_t)tr * nmodes + (int64_t)ms0 * (iy + (int64_t)ms1 * iz);
+  const int x1 = min(ms0, x0 + DC_X);
+  for (int ix = x0 + threadIdx.x; ix < x1; ix += DC_THREADS) {
     const int kx = mode_of(ix, ms0, modeord);
-    int64_t g = kx >= 0 ? kx : nf0 + kx;
-    T f = i0[kx >= 0 ? kx : -kx];
-    if (DIM > 1) {
-      const int iy = (int)((i / ms0) % ms1);
-      const int ky = mode_of(iy, ms1, modeord);
-      g += (int64_t)nf0 * (ky >= 0 ? ky : nf1 + ky);
-      f *= i1[ky >= 0 ? ky : -ky];
-    }
-    if (DIM > 2) {
-      const int iz = (int)(i / ((int64_t)ms0 * ms1));
-      const int kz = mode_of(iz, ms2, modeord);
-      g += (int64_t)nf0 * nf1 * (kz >= 0 ? kz : nf2 + kz);
-      f *= i2[kz >= 0 ? kz : -kz];
-    }
-    const cplx<T> v = fw[(int64_t)tr * nf_total + g];
+    const cplx<T> v = fw[grow + (kx >= 0 ? kx : nf0 + kx)];
+    const T f = fyz * i0[kx >= 0 ? kx : -kx];
     cplx<T> r;
     r.x = v.x * f;
     r.y = v.y * f;
-    fk[q] = r;
+    fk[orow + ix] = r;
   }
 }
 
+// fw[t][g] = fk[t][mode(g)] / prod phihat for retained modes, 0 elsewhere (type 2)
 template <typename T, int DIM>
-__global__ void amplify_kernel(int ms0, int ms1, int ms2, int nf0, int nf1, int nf2, int modeord,
-                               const T *__restrict__ i0, const T *__restrict__ i1,
-                               const T *__restrict__ i2, const cplx<T> *__restrict__ fk,
-                               int64_t nmodes, cplx<T> *__restrict__ fw, int64_t nf_total,
-                               int ntr) {
-  const int64_t total = nf_total * ntr;
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
-       q += (int64_t)gridDim.x * blockDim.x) {
-    const int tr = (int)(q / nf_total);
-    const int64_t g = q - (int64_t)tr * nf_total;
+__global__ void __launch_bounds__(DC_THREADS)
+    amplify_kernel(int ms0, int ms1, int ms2, int nf0, int nf1, int nf2, int modeord,
+                   const T *__restrict__ i0, const T *__restrict__ i1, const T *__restrict__ i2,
+                   const cplx<T> *__restrict__ fk, int64_t nmodes, cplx<T> *__restrict__ fw,
+                   int64_t nf_total, int xchunks) {
+  const int row = blockIdx.x / xchunks;
+  const int x0 = (blockIdx.x - row * xchunks) * DC_X;
+  int gy = 0, gz = 0, tr = row;
+  if (DIM > 1) {
+    gy = row % nf1;
+    tr = row / nf1;
+  }
+  if (DIM > 2) {
+    gz = tr % nf2;
+    tr /= nf2;
+  }
+  bool in = true;
+  T fyz = T(1);
+  int64_t irow = (int64_t)tr * nmodes;
+  if (DIM > 1) {
+    const int ky = gy <= (ms1 - 1) / 2 ? gy : (gy >= nf1 - ms1 / 2 ? gy - nf1 : INT32_MIN);
+    in = ky != INT32_MIN;
+    if (in) {
+      irow += (int64_t)ms0 * pos_of(ky, ms1, modeord);
+      fyz = i1[ky >= 0 ? ky : -ky];
+    }
+  }
+  if (DIM > 2 && in) {
+    const int kz = gz <= (ms2 - 1) / 2 ? gz : (gz >= nf2 - ms2 / 2 ? gz - nf2 : INT32_MIN);
+    in = kz != INT32_MIN;
+    if (in) {
+      irow += (int64_t)ms0 * ms1 * pos_of(kz, ms2, modeord);
+      fyz *= i2[kz >= 0 ? kz : -kz];
+    }
+  }
+  const int64_t grow = (int64_t)tr * nf_total + (int64_t)nf0 * (gy + (int64_t)nf1 * gz);
+  const int x1 = min(nf0, x0 + DC_X);
+  for (int gx = x0 + threadIdx.x; gx < x1; gx += DC_THREADS) {
     cplx<T> r;
     r.x = T(0);
     r.y = T(0);
-    bool in = true;
-    const int gx = (int)(g % nf0);
-    int kx = gx <= (ms0 - 1) / 2 ? gx : (gx >= nf0 - ms0 / 2 ? gx - nf0 : INT32_MIN);
-    in = kx != INT32_MIN;
-    int ky = 0, kz = 0;
-    if (DIM > 1 && in) {
-      const int gy = (int)((g / nf0) % nf1);
-      ky = gy <= (ms1 - 1) / 2 ? gy : (gy >= nf1 - ms1 / 2 ? gy - nf1 : INT32_MIN);
-      in = ky != INT32_MIN;
-    }
-    if (DIM > 2 && in) {
-      const int gz = (int)(g / ((int64_t)nf0 * nf1));
-      kz = gz <= (ms2 - 1) / 2 ? gz : (gz >= nf2 - ms2 / 2 ? gz - nf2 : INT32_MIN);
-      in = kz != INT32_MIN;
-    }
     if (in) {
-      int64_t i = pos_of(kx, ms0, modeord);
-      T f = i0[kx >= 0 ? kx : -kx];
-      if (DIM > 1) {
-        i += (int64_t)ms0 * pos_of(ky, ms1, modeord);
-        f *= i1[ky >= 0 ? ky : -ky];
+      const int kx = gx <= (ms0 - 1) / 2 ? gx : (gx >= nf0 - ms0 / 2 ? gx - nf0 : INT32_MIN);
+      if (kx != INT32_MIN) {
+        const cplx<T> v = fk[irow + pos_of(kx, ms0, modeord)];
+        const T f = fyz * i0[kx >= 0 ? kx : -kx];
+        r.x = v.x * f;
+        r.y = v.y * f;
       }
-      if (DIM > 2) {
-        i += (int64_t)ms0 * ms1 * pos_of(kz, ms2, modeord);
-        f *= i2[kz >= 0 ? kz : -kz];
-      }
-      const cplx<T> v = fk[(int64_t)tr * nmodes + i];
-      r.x = v.x * f;
-      r.y = v.y * f;
     }
-    fw[q] = r;
+    fw[grow + gx] = r;
   }
 }
 
@@ -304,16 +337,24 @@ template <typename T>
 void launch_deconv(int dim, const int ms[3], const int nf[3], int modeord, const T *const inv[3],
                    const cplx<T> *fw, int64_t nf_total, cplx<T> *fk, int ntr, cudaStream_t s) {
   const int64_t nmodes = (int64_t)ms[0] * ms[1] * ms[2];
-  const unsigned g = blocks_for(nmodes * ntr, 256);
+  const int xchunks = (ms[0] + DC_X - 1) / DC_X;
+  const int64_t blocks = (int64_t)xchunks * ms[1] * ms[2] * ntr;
+  if (blocks <= 0) return;
+  if (blocks > std::numeric_limits<int32_t>::max())
+    GBN_THROW(FINUFFT_ERR_MAXNALLOC, "deconvolution grid");
+  const unsigned g = (unsigned)blocks;
   if (dim == 1)
-    deconv_kernel<T, 1><<<g, 256, 0, s>>>(ms[0], 1, 1, nf[0], 1, 1, modeord, inv[0], inv[0],
-                                          inv[0], fw, nf_total, fk, nmodes, ntr);
+    deconv_kernel<T, 1><<<g, DC_THREADS, 0, s>>>(ms[0], 1, 1, nf[0], 1, 1, modeord, inv[0],
+                                                 inv[0], inv[0], fw, nf_total, fk, nmodes,
+                                                 xchunks);
   else if (dim == 2)
-    deconv_kernel<T, 2><<<g, 256, 0, s>>>(ms[0], ms[1], 1, nf[0], nf[1], 1, modeord, inv[0],
-                                          inv[1], inv[1], fw, nf_total, fk, nmodes, ntr);
+    deconv_kernel<T, 2><<<g, DC_THREADS, 0, s>>>(ms[0], ms[1], 1, nf[0], nf[1], 1, modeord,
+                                                 inv[0], inv[1], inv[1], fw, nf_total, fk,
+                                                 nmodes, xchunks);
   else
-    deconv_kernel<T, 3><<<g, 256, 0, s>>>(ms[0], ms[1], ms[2], nf[0], nf[1], nf[2], modeord,
-                                          inv[0], inv[1], inv[2], fw, nf_total, fk, nmodes, ntr);
+    deconv_kernel<T, 3><<<g, DC_THREADS, 0, s>>>(ms[0], ms[1], ms[2], nf[0], nf[1], nf[2],
+                                                 modeord, inv[0], inv[1], inv[2], fw, nf_total,
+                                                 fk, nmodes, xchunks);
   GBN_LAUNCH_CHECK();
 }
 
@@ -322,16 +363,24 @@ void launch_amplify(int dim, const int ms[3], const int nf[3], int modeord,
                     const T *const inv[3], const cplx<T> *fk, cplx<T> *fw, int64_t nf_total,
                     int ntr, cudaStream_t s) {
   const int64_t nmodes = (int64_t)ms[0] * ms[1] * ms[2];
-  const unsigned g = blocks_for(nf_total * ntr, 256);
+  const int xchunks = (nf[0] + DC_X - 1) / DC_X;
+  const int64_t blocks = (int64_t)xchunks * nf[1] * nf[2] * ntr;
+  if (blocks <= 0) return;
+  if (blocks > std::numeric_limits<int32_t>::max())
+    GBN_THROW(FINUFFT_ERR_MAXNALLOC, "amplification grid");
+  const unsigned g = (unsigned)blocks;
   if (dim == 1)
-    amplify_kernel<T, 1><<<g, 256, 0, s>>>(ms[0], 1, 1, nf[0], 1, 1, modeord, inv[0], inv[0],
-                                           inv[0], fk, nmodes, fw, nf_total, ntr);
+    amplify_kernel<T, 1><<<g, DC_THREADS, 0, s>>>(ms[0], 1, 1, nf[0], 1, 1, modeord, inv[0],
+                                                  inv[0], inv[0], fk, nmodes, fw, nf_total,
+                                                  xchunks);
   else if (dim == 2)
-    amplify_kernel<T, 2><<<g, 256, 0, s>>>(ms[0], ms[1], 1, nf[0], nf[1], 1, modeord, inv[0],
-                                           inv[1], inv[1], fk, nmodes, fw, nf_total, ntr);
+    amplify_kernel<T, 2><<<g, DC_THREADS, 0, s>>>(ms[0], ms[1], 1, nf[0], nf[1], 1, modeord,
+                                                  inv[0], inv[1], inv[1], fk, nmodes, fw,
+                                                  nf_total, xchunks);
   else
-    amplify_kernel<T, 3><<<g, 256, 0, s>>>(ms[0], ms[1], ms[2], nf[0], nf[1], nf[2], modeord,
-                                           inv[0], inv[1], inv[2], fk, nmodes, fw, nf_total, ntr);
+    amplify_kernel<T, 3><<<g, DC_THREADS, 0, s>>>(ms[0], ms[1], ms[2], nf[0], nf[1], nf[2],
+                                                  modeord, inv[0], inv[1], inv[2], fk, nmodes,
+                                                  fw, nf_total, xchunks);
   GBN_LAUNCH_CHECK();
 }
 

@@ -139,6 +139,17 @@ template <typename T> void Plan<T>::make_grid() {
   nf_total = (int64_t)nf[0] * nf[1] * nf[2];
   choose_spread_config(opts.gpu_method != 0);
   if (!opts.gpu_spreadinterponly) {
+    // transforms per batch at most as many as keep their fine grids within half
+    // of L2: a grid that stays in L2 from spread (or amplification) through the
+    // FFT to deconvolution (or interpolation) never travels to HBM (measured on
+    // 16 vectors of 1e7 2D type-2 points, 2048^2 grids: batches of 16 6.6 ms,
+    // of 1 4.8 ms per execute). gpu_maxbatchsize is an upper bound.
+    int dev = 0, l2 = 0;
+    GBN_CUDA(cudaGetDevice(&dev));
+    GBN_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+    const double gbytes = (double)nf_total * sizeof(cplx<T>);
+    if (2.0 * gbytes <= (double)l2)
+      batchsize = std::min(batchsize, std::max(1, (int)((double)l2 / (2.0 * gbytes))));
     destroy_fft();
     fw.resize((size_t)nf_total * batchsize);
     make_fft();
@@ -219,7 +230,22 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
   if (dim == 3 && (bins[0] > 1000 || bins[1] > 1000 || bins[2] > 1000))
     GBN_THROW(FINUFFT_ERR_BINSIZE_NOTVALID, "3D bins must be < 1000");
   if (opts.gpu_maxsubprobsize < 1) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "maxsubprobsize");
-  S.method = opts.gpu_method == 0 ? 2 : (opts.gpu_method == 1 ? 1 : 2);
+  // methods: 1 global atomics, 2 shared-memory tiles (also for 4, the reference's
+  // block-gather, accepted for compatibility), 3 output-driven tiles
+  S.method = opts.gpu_method == 0 ? 2 : (opts.gpu_method == 1 ? 1 : (opts.gpu_method == 3 ? 3 : 2));
+  if (S.method == 3) {
+    S.smem = spread_output_driven_bytes<T>(dim, ns, bins);
+    if (S.smem > (size_t)limit) {
+      fprintf(stderr, "[gbnufft] output-driven tile needs %zu bytes of shared memory, %d "
+                      "available\n", S.smem, limit);
+      GBN_THROW(FINUFFT_ERR_INSUFFICIENT_SHMEM, "tile too large");
+    }
+    S.cfg.method = 3;
+    S.cfg.threads = 256;
+    S.cfg.smem = S.smem;
+    S.cfg.variant = 0;
+    return S;
+  }
   S.smem = spread_tile_smem<T>(dim, ns, bins, threads);
   if (S.method == 2 && S.smem > (size_t)limit) {
     if (user_method) {
@@ -403,14 +429,24 @@ template <typename T> void Plan<T>::make_fseries() {
 
 // ---------------------------------------------------------- planners 2, 3 ----
 template <typename T> bool Plan<T>::candidate_valid(const Candidate &c) const {
-  // analytic rejection: the PSWF width law's width for tol at this sigma must
-  // fit the precision's widest kernel, so the kernel's aliasing bound reaches tol
+  // analytic rejection: the kernel width for tol at this sigma -- the larger of
+  // the PSWF width law and the GPU rule, as the plan would pick it -- must fit
+  // the precision's widest kernel (unclipped, the law's aliasing bound reaches
+  // tol). In single precision a sigma below 2 also needs tol >= 1e-5: the
+  // larger range of 1/phihat lifts the float rounding above the tolerance
+  // below that (the engine's own timing and error sweeps: 16% of the sigma-1.5
+  // float plans at tol < 1e-5 had errors above 2 tol, none at sigma 2).
   const bool is_float = std::is_same_v<T, float>;
   const double t = std::max(tol, is_float ? (double)FLT_EPSILON : DBL_EPSILON);
   const double tolfac = 0.18 * std::pow(1.4, dim - 1) * (type == 3 ? 1.4 : 1.0);
-  const int ns = (int)std::ceil(std::log(tolfac / t) / (PI * std::sqrt(1.0 - 1.0 / c.sigma)) + 1.0);
+  const double u = PI * std::sqrt(1.0 - 1.0 / c.sigma);
+  const int ns_law = (int)std::ceil(std::log(tolfac / t) / u + 1.0);
+  const int ns_gpu = c.sigma == 2.0 ? (int)std::ceil(-std::log10(t / 10.0))
+                                    : (int)std::ceil(-std::log(t) / u);
+  const int ns = std::max(2, std::max(ns_law, ns_gpu));
   const int maxns = is_float ? MAX_NS_FLOAT : MAX_NS;
-  return ns <= maxns && kernel_tol_bound(std::max(ns, 2), c.sigma, dim, type) <= t * (1 + 1e-9);
+  if (is_float && c.sigma < 2.0 && tol < 1e-5) return false;
+  return ns <= maxns && kernel_tol_bound(ns, c.sigma, dim, type) <= t * (1 + 1e-9);
 }
 
 template <typename T> void Plan<T>::apply_sigma(double sigma) {

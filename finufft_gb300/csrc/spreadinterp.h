@@ -5,7 +5,8 @@
 namespace gbn {
 
 struct SpreadConfig {
-  int method;       // 1: point-driven global atomics, 2: tiled shared memory
+  int method;       // 1: point-driven global atomics, 2: tiled shared memory,
+                    // 3: output-driven tiles (one writer per cell)
   int threads;      // CTA size
   size_t smem;      // dynamic shared memory bytes for method 2
   int variant = 0;  // 3D method 2: 0 shared tile + atomics, 1 exclusive warp tiles
@@ -21,6 +22,8 @@ template <typename T> size_t spread_tile2m_bytes(int ns, const int bin[3], int w
 template <typename T> size_t spread_tile3v_bytes(int ns, const int bin[3], int warps);
 // Shared-memory bytes of the warp-aggregated 3D spread (variant 2).
 template <typename T> size_t spread_tile3m_bytes(int ns, const int bin[3], int warps);
+// Shared-memory bytes of the output-driven spread (method 3).
+template <typename T> size_t spread_output_driven_bytes(int dim, int ns, const int bin[3]);
 // Shared-memory bytes of the double-precision int64 fixed-point 3D spread (variant 4).
 size_t spread_tile3x_bytes(int ns, const int bin[3], int warps);
 

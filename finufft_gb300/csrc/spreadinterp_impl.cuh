@@ -207,6 +207,99 @@ __global__ void __launch_bounds__(256)
 }
 
 // ---------------------------------------------------------------------------
+// Method 3, output-driven spreading (the reference's gpu_method 3,
+// src/cuda/spread_output_driven_inst.cu:17-158): the subproblem's points are
+// staged in batches of OD_BATCH with their kernel weights, then taken one at a
+// time, the block's threads splitting that point's ns^d support cells among
+// themselves, so every cell has one writer and the tile takes plain adds (a
+// block barrier between points); the tile is then added into the grid.
+constexpr int OD_BATCH = 64;
+constexpr int OD_THREADS = 256;
+
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(OD_THREADS)
+    spread_output_driven_kernel(PointLayout<T> L0, KernelShape<T> K,
+                                const cplx<T> *__restrict__ c, const cplx<T> *__restrict__ pre,
+                                int conj_pre, cplx<T> *__restrict__ fw, int64_t nf_total) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int sub = blockIdx.x;
+  const int tr = blockIdx.y;
+  int b = L0.sub_bin[sub];
+  PointLayout<T> Lg;
+  const int64_t goff = resolve_problem<T>(L0, Lg, b);
+  const PointLayout<T> &L = Lg;
+  const int p0 = L.sub_start[sub];
+  const int np = L.sub_count[sub];
+  const TileGeom<DIM> G = tile_of<T, DIM, NS>(L, b);
+  T *re = reinterpret_cast<T *>(smem_raw);
+  T *im = re + G.cells;
+  T *kw = im + G.cells;                        // [OD_BATCH][DIM][NS]
+  T *vr = kw + OD_BATCH * DIM * NS;            // [OD_BATCH]
+  T *vi = vr + OD_BATCH;                       // [OD_BATCH]
+  int *st = reinterpret_cast<int *>(vi + OD_BATCH); // [OD_BATCH][DIM] start cells
+  for (int i = threadIdx.x; i < G.cells; i += blockDim.x) {
+    re[i] = T(0);
+    im[i] = T(0);
+  }
+  const cplx<T> *ct = c + (int64_t)tr * L.M;
+  constexpr int TOTAL = DIM == 1 ? NS : (DIM == 2 ? NS * NS : NS * NS * NS);
+  for (int b0 = 0; b0 < np; b0 += OD_BATCH) {
+    const int nb = min(OD_BATCH, np - b0);
+    __syncthreads(); // the previous batch's readers are done (and the tile is zeroed)
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+      const int p = p0 + b0 + i;
+      const int j = L.perm[p];
+      cplx<T> v = ct[j];
+      if (pre) v = cmul_opt<T>(v, pre[j], conj_pre);
+      vr[i] = v.x;
+      vi[i] = v.y;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        T kk[NS];
+        st[i * DIM + d] = point_weights<T, NS>(L.loc[d][p], L.bin[d], K, kk);
+#pragma unroll
+        for (int a = 0; a < NS; ++a) kw[(i * DIM + d) * NS + a] = kk[a];
+      }
+    }
+    __syncthreads();
+    for (int i = 0; i < nb; ++i) {
+      const T *k = kw + i * DIM * NS;
+      for (int idx = threadIdx.x; idx < TOTAL; idx += blockDim.x) {
+        const int dx = idx % NS;
+        int t = dx + st[i * DIM];
+        T w = k[dx];
+        if (DIM > 1) {
+          const int dy = (idx / NS) % NS;
+          w *= k[NS + dy];
+          t += G.t[0] * (dy + st[i * DIM + 1]);
+        }
+        if (DIM > 2) {
+          const int dz = idx / (NS * NS);
+          w *= k[2 * NS + dz];
+          t += G.t[0] * G.t[1] * (dz + st[i * DIM + 2]);
+        }
+        re[t] += vr[i] * w;
+        im[t] += vi[i] * w;
+      }
+      __syncthreads(); // the next point's support may overlap this one's
+    }
+  }
+  __syncthreads();
+  cplx<T> *fwt = fw + (int64_t)tr * nf_total + goff;
+  for (int q = threadIdx.x; q < G.cells; q += blockDim.x) {
+    cplx<T> v;
+    v.x = re[q];
+    v.y = im[q];
+    if (v.x == T(0) && v.y == T(0)) continue;
+    const int x = q % G.t[0];
+    int64_t g = wrap_idx(G.org[0] + x, L.nf[0]);
+    if (DIM > 1) g += (int64_t)L.nf[0] * wrap_idx(G.org[1] + (q / G.t[0]) % G.t[1], L.nf[1]);
+    if (DIM > 2) g += (int64_t)L.nf[0] * L.nf[1] * wrap_idx(G.org[2] + q / (G.t[0] * G.t[1]), L.nf[2]);
+    atomic_add_cplx_global(fwt + g, v);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Method 2 in 3D: tiled spreading with warp-cooperative, bank-conflict-free
 // shared-memory atomics.
 //  * Each warp takes 32 points at a time: lane l loads point l (coalesced),
@@ -1832,6 +1925,14 @@ template <typename T, int DIM> struct Dispatch {
                      const cplx<T> *pre, int conj_pre, cplx<T> *fw, int64_t nf_total, int ntr,
                      const SpreadConfig &cfg, cudaStream_t s) {
     dim3 grid((unsigned)L.nsub, (unsigned)ntr);
+    if (cfg.method == 3) {
+      auto ko = spread_output_driven_kernel<T, DIM, NS>;
+      GBN_CUDA(cudaFuncSetAttribute(ko, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)cfg.smem));
+      ko<<<grid, OD_THREADS, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
+      GBN_LAUNCH_CHECK();
+      return;
+    }
     if (cfg.method == 1) {
       spread_global_kernel<T, DIM, NS><<<grid, GLOBAL_SPREAD_THREADS, 0, s>>>(L, K, c, pre, conj_pre, fw,
                                                                     nf_total);

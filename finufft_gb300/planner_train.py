@@ -132,7 +132,11 @@ def main():
             json.dump(rep, f, indent=1)
     lo = F.min(0) - 0.25 * np.abs(F.min(0)) - 0.5
     hi = F.max(0) + 0.25 * np.abs(F.max(0)) + 0.5
-    fmt = lambda a: ", ".join("%.9gf" % v for v in a)
+    def lit(v):
+        t = "%.9g" % v
+        return (t if any(ch in t for ch in ".en") else t + ".0") + "f"
+
+    fmt = lambda a: ", ".join(lit(v) for v in a)
     lines = [
         "// Trained weights of the learned planner (2x64 MLP), written by",
         "// python -m finufft_gb300.planner_train from %d engine sweeps (%d held out)." % (n, ntest),
@@ -144,7 +148,7 @@ def main():
         "static const float kPlannerStd[PLANNER_NF] = {%s};" % fmt(std),
         "static const float kPlannerLo[PLANNER_NF] = {%s};" % fmt(lo),
         "static const float kPlannerHi[PLANNER_NF] = {%s};" % fmt(hi),
-        "static const float kPlannerYMean = %.9gf, kPlannerYStd = %.9gf;" % (ymean, ystd),
+        "static const float kPlannerYMean = %s, kPlannerYStd = %s;" % (lit(ymean), lit(ystd)),
         "__device__ float g_planner_w[PLANNER_NW] = {",
     ]
     for i in range(0, NW, 8):
