@@ -38,12 +38,23 @@ void *g_scratch_addr[MAX_DEVICES] = {};
 
 // Device address of the scratch array on the current device. In host code
 // the array's name is only a host-side stand-in, so the address is looked up
-// once per device (with that device current) and cached.
+// once per device (with that device current) and cached. The cached address
+// is checked at every call: after a reset of the device's context the module
+// is loaded again and the array may move, so an address the runtime no longer
+// knows as device memory of this device is looked up again.
 void *scratch_address() {
   int dev = 0;
   GBN_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= MAX_DEVICES) GBN_THROW(FINUFFT_ERR_CUDA_FAILURE, "device index");
   std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (g_scratch_addr[dev]) {
+    cudaPointerAttributes a{};
+    const cudaError_t e = cudaPointerGetAttributes(&a, g_scratch_addr[dev]);
+    if (e != cudaSuccess || a.type != cudaMemoryTypeDevice || a.device != dev) {
+      cudaGetLastError();
+      g_scratch_addr[dev] = nullptr;
+    }
+  }
   if (!g_scratch_addr[dev]) {
     void *ptr = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
@@ -107,9 +118,15 @@ int spread_noalloc_f(int dim, const int64_t *n_grid, int64_t M, const float *x, 
     for (int d = 0; d < dim; ++d) loc[d] = (float *)arena.take(mb * 4);
     for (int d = dim; d < 3; ++d) loc[d] = loc[0];
 
+    // sort keys as a plan's (Plan::sort_points): bin and cell, for odd widths
+    // bin and start cell of the support (bin + 1 values per dimension)
     const int nb = S.nbins[0] * S.nbins[1] * S.nbins[2];
-    const uint64_t binvol = (uint64_t)S.bins[0] * S.bins[1] * S.bins[2];
-    const int cell_keys = (uint64_t)nb * binvol <= 0xffffffffull ? 1 : 0;
+    const uint64_t binvol0 = (uint64_t)S.bins[0] * S.bins[1] * S.bins[2];
+    uint64_t sbinvol = 1;
+    for (int d = 0; d < dim; ++d) sbinvol *= (uint64_t)S.bins[d] + 1;
+    int cell_keys = (uint64_t)nb * binvol0 <= 0xffffffffull ? 1 : 0;
+    if (cell_keys && kc.ns % 2 == 1 && (uint64_t)nb * sbinvol <= 0xffffffffull) cell_keys = 2;
+    const uint64_t binvol = cell_keys == 2 ? sbinvol : binvol0;
     const uint64_t nkeys = cell_keys ? (uint64_t)nb * binvol : (uint64_t)nb;
     int keybits = 0;
     while ((1ull << keybits) < nkeys) ++keybits;
@@ -141,7 +158,7 @@ int spread_noalloc_f(int dim, const int64_t *n_grid, int64_t M, const float *x, 
     L.sub_start = sa.start;
     L.sub_count = sa.count;
     L.perm = perm;
-    L.cell_sorted = cell_keys;
+    L.cell_sorted = cell_keys ? 1 : 0;
     launch_spread<float>(L, K, c, nullptr, 0, grid, cells, 1, S.cfg, stream);
     GBN_CUDA(cudaGetLastError());
     return 0;

@@ -73,3 +73,44 @@ def test_noalloc_rejects_oversize(engine):
     m1 = (ctypes.c_int64 * 3)(1024, 1, 1)
     assert engine.cufinufftf_spread_noalloc(1, m1, (1 << 19) + 1, None, None, None, None, None,
                                             1e-5, None) == 2
+
+
+def _free_bytes():
+    import torch
+
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info()[0]
+
+
+def test_noalloc_at_the_limits_against_the_oracle(engine, oracle):
+    """3D at the declared limits (2^19 points, 2^24 grid cells, an odd kernel
+    width whose start-cell sort keys are used too): the output equals the
+    oracle's FP64 spread with the same ES kernel, and the call leaves the
+    device's free memory unchanged (nothing allocated: the scratch is the fixed
+    array, the library's setpts pool is trimmed first)"""
+    import torch
+
+    rng = np.random.default_rng(91)
+    M = 1 << 19
+    nm_c = (256, 256, 256)  # 2^24 cells, x fastest
+    pts = rng.uniform(-np.pi, np.pi, (3, M)).astype(np.float32)
+    pts[:, : M // 2] = (0.3 * rng.standard_normal((3, M // 2))).astype(np.float32)
+    c = (rng.standard_normal(M) + 1j * rng.standard_normal(M)).astype(np.complex64)
+    pts_c = [torch.from_numpy(p).cuda() for p in pts]
+    cd = torch.from_numpy(c).cuda()
+    grid = torch.empty(1 << 24, dtype=torch.complex64, device="cuda")
+    m = (ctypes.c_int64 * 3)(*nm_c)
+    for tol in (1e-5, 1e-4):  # widths 6 and 5
+        assert engine.cufinufftf_spread_noalloc(3, m, M, *[a.data_ptr() for a in pts_c],
+                                                cd.data_ptr(), grid.data_ptr(), tol, None) == 0
+        assert engine.gbnufft_trim_scratch(0) == 0
+        free0 = _free_bytes()
+        assert engine.cufinufftf_spread_noalloc(3, m, M, *[a.data_ptr() for a in pts_c],
+                                                cd.data_ptr(), grid.data_ptr(), tol, None) == 0
+        free1 = _free_bytes()
+        assert free1 >= free0, (free0, free1)
+        got = grid.cpu().numpy()
+        ns, beta = oracle.gpu_kernel(tol, 2.0, 1, True)
+        want = oracle._spread([p.astype(np.float64) for p in pts], c, list(nm_c), ns, beta).ravel()
+        err = np.linalg.norm(got - want) / np.linalg.norm(want)
+        assert err < 1e-5, (tol, err)
