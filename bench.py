@@ -399,6 +399,9 @@ def run_gpu(args):
     lib.finufftf_destroy(hplan)
     del hc, hf
 
+    # the reference cuFINUFFT compiled for this GPU, same inputs, default options
+    ref_gpu = reference_gpu_type1(x, y, z, c, nt, stream, args, dev)
+
     # roofline of the dominant kernel (spread): shared-memory adds
     ns = binfo.ns
     atom_per_launch = float(M) * nt * 2 * ns ** 3
@@ -477,6 +480,7 @@ def run_gpu(args):
         "accuracy": {"rel_l2_vs_fp64_direct": acc,
                      "sample": "1e3 modes: seeded 10x10x10 grid of mode indices, vector 0",
                      "ratio_batched_over_cpu": (acc["batched"] / acc["cpu"]) if "cpu" in acc else None},
+        "reference_gpu": ref_gpu,
         "e2e": {"value": job_value(M * nt, world, ms_e2e), "unit": "NU pts/s",
                 "h2d_bytes_per_step": nt * M * 8, "d2h_bytes_per_step": nt * int(np.prod(N_MODES)) * 8,
                 "api": "finufftf_execute (host pointers, pinned)", "rel_diff_vs_device_api": e2e_err},
@@ -514,6 +518,70 @@ def run_gpu(args):
 
 
 # ------------------------------------------------------ the other workloads ----
+REF_GPU_LIB = os.path.join(ROOT, "baseline", "_ref", "cufinufft", "libcufinufft_ref.so")
+
+
+def reference_gpu_type1(x, y, z, c, nt, stream, args, dev):
+    """The reference cuFINUFFT (its src/cuda compiled for sm_103a by
+    oracle/Makefile target ref-gpu) on the same device inputs through its own C
+    API with default options: one vector, and the nt vectors as one plan
+    (its batching). Execute timed with CUDA events on the same stream."""
+    import ctypes
+
+    import torch
+
+    from finufft_gb300 import _lib
+
+    if not os.path.exists(REF_GPU_LIB):
+        return {"unavailable": "reference cuFINUFFT not built for this GPU (oracle/Makefile "
+                               "targets ref-gpu-src, ref-gpu)"}
+    try:
+        L = ctypes.CDLL(REF_GPU_LIB)  # its own namespace: RTLD_LOCAL
+        P = ctypes.c_void_p
+        L.cufinufft_default_opts.argtypes = [ctypes.POINTER(_lib.CufinufftOpts)]
+        L.cufinufftf_makeplan.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                          ctypes.POINTER(P), ctypes.POINTER(_lib.CufinufftOpts)]
+        L.cufinufftf_setpts.argtypes = [P, ctypes.c_int64, P, P, P, ctypes.c_int, P, P, P]
+        L.cufinufftf_execute.argtypes = [P, P, P]
+        L.cufinufftf_destroy.argtypes = [P]
+        out = {"library": "reference cuFINUFFT (src/cuda) built for sm_103a, default options"}
+        M = x.numel()
+        N = list(N_MODES)
+        for name, ntr in (("plain", 1), ("batched", nt)):
+            o = _lib.CufinufftOpts()
+            L.cufinufft_default_opts(ctypes.byref(o))
+            o.gpu_stream = stream.cuda_stream
+            plan = P()
+            nm = (ctypes.c_int64 * 3)(N[2], N[1], N[0])  # x fastest
+            rc = L.cufinufftf_makeplan(1, 3, nm, 1, ntr, TOL, ctypes.byref(plan), ctypes.byref(o))
+            if rc != 0:
+                out[name] = {"error": "makeplan %d" % rc}
+                continue
+            # its fastest axis is the last array axis: pass (z, y, x)
+            t0 = time.perf_counter()
+            rc = L.cufinufftf_setpts(plan, M, z.data_ptr(), y.data_ptr(), x.data_ptr(), 0, None,
+                                     None, None)
+            torch.cuda.synchronize()
+            setpts_s = time.perf_counter() - t0
+            cc = c[0].contiguous() if ntr == 1 else c
+            fk = torch.empty((ntr,) + tuple(N), dtype=torch.complex64, device=dev)
+            ms = time_steps(lambda: L.cufinufftf_execute(plan, cc.data_ptr(), fk.data_ptr()),
+                            stream, max(1, args.steps // 2), min(args.warmup, 2))
+            ent = {"value": M * ntr / (ms * 1e-3), "ms_per_step": ms, "setpts_s": setpts_s}
+            if ntr == 1:
+                ax = sample_axes(N_MODES, 10, 5)
+                ref = direct_type1_grid([x, y, z], c[0], N_MODES, ax, +1, dev)
+                ent["rel_l2_vs_fp64_direct"] = rel_l2(take_grid(fk[0], ax), ref)
+            out[name] = ent
+            L.cufinufftf_destroy(plan)
+            del fk
+            torch.cuda.empty_cache()
+        return out
+    except Exception as e:  # the baseline must not take the metric line down
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
 def cfg_c1(args, dev, stream, with_cpu=True):
     """C1: 1D type 1 FP64, M = N = 1e6, tol 1e-9 (the reference's CPU-runnable case)"""
     import torch

@@ -87,8 +87,18 @@ __global__ void __launch_bounds__(INTERP_TMA_THREADS)
   const int bz = DIM == 3 ? BZ : 1;
   const uint32_t box_bytes = (uint32_t)(BX * BY * bz) * (uint32_t)sizeof(cplx<T>);
   const uint32_t buf_stride = (box_bytes + 127u) / 128u * 128u;
-  cplx<T> *buf0 = reinterpret_cast<cplx<T> *>(smem_raw);
-  const uint32_t sbuf0 = smem_addr(smem_raw);
+  // the copies' destinations must be 128-byte aligned: the dynamic buffer is
+  // aligned here (the launch reserves 128 bytes of slack), whatever alignment
+  // the shared-memory layout gave it; a misaligned result leaves the block on
+  // per-thread loads and records the error
+  const uint32_t sraw = smem_addr(smem_raw);
+  const uint32_t pad = (128u - (sraw & 127u)) & 127u;
+  unsigned char *sm = smem_raw + pad;
+  const uint32_t sbuf0 = sraw + pad;
+  if ((sbuf0 & 127u) != 0u) {
+    if (threadIdx.x == 0) atomicExch(err, 2);
+    interior = false;
+  }
   const uint32_t bar[2] = {smem_addr(&bars[0]), smem_addr(&bars[1])};
   if (interior && threadIdx.x == 0) {
     mbar_init(bar[0], 1);
@@ -135,7 +145,7 @@ __global__ void __launch_bounds__(INTERP_TMA_THREADS)
     }
     for (int k = 0; k < ntr; ++k) {
       const int s = k & 1;
-      cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw + s * buf_stride);
+      cplx<T> *buf = reinterpret_cast<cplx<T> *>(sm + s * buf_stride);
       if (interior) {
         if (threadIdx.x == 0) {
           if (k == 0) issue(0);

@@ -2007,7 +2007,7 @@ template <typename T, int DIM> struct Dispatch {
         const int BX = (t0 + 2) & ~1; // even, at least t0 + 1
         const int xm = sizeof(T) == 8 ? 2 : 1;
         const size_t box = (size_t)BX * t1 * t2 * sizeof(cplx<T>);
-        const size_t smem = 2 * ((box + 127) / 128 * 128);
+        const size_t smem = 2 * ((box + 127) / 128 * 128) + 128; // + alignment slack
         CUtensorMap map;
         if (BX * xm <= 256 && t1 <= 256 && t2 <= 256 && BX <= L.nf[0] && smem <= 100 * 1024 &&
             encode_grid_map<T>(&map, fw, DIM, L.nf, ntr, BX, t1, t2)) {
