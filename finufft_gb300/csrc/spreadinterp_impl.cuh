@@ -467,7 +467,7 @@ __global__ void __launch_bounds__(256)
   __shared__ double red[8];
   __shared__ int mode; // 0: fixed point, 1: double atomics
   __shared__ double inv_scale;
-  __shared__ float scale_f;
+  __shared__ double scale_d;
   constexpr int SK = STAGE_STRIDE;
   constexpr int NXB = (NS + 7) / 8;
   constexpr int NPAIR = NS * NS;
@@ -525,18 +525,23 @@ __global__ void __launch_bounds__(256)
     int e = 0;
     mode = 0;
     if (!(S < 1e300)) {
-      mode = 1; // inf or NaN strengths: keep IEEE propagation
+      mode = 1; // inf or NaN strengths: keep IEEE propagation (scale 1)
     } else if (S > 0.0) {
       e = 62 - (int)ceil(log2(1.01 * S));
-      // 2^e must be a normal float, as must the staged scaled strengths
-      if (e > 120 || e < -126) mode = 1;
+      // 2^e must be a normal float, as must the staged scaled strengths;
+      // otherwise double atomics on strengths scaled to at most 1 in magnitude
+      // (staged as float pairs without overflow or underflow)
+      if (e > 120 || e < -126) {
+        mode = 1;
+        e = -(int)ceil(log2(S));
+      }
     }
-    scale_f = mode ? 1.0f : __int_as_float((e + 127) << 23); // 2^e
-    inv_scale = mode ? 1.0 : ldexp(1.0, -e);
+    scale_d = ldexp(1.0, e);
+    inv_scale = ldexp(1.0, -e);
   }
   __syncthreads();
   const bool fx = mode == 0;
-  const double sc = fx ? (double)scale_f : 1.0;
+  const double sc = scale_d;
   const int lx = lane & 7, lp = lane >> 3;
   for (int base = warp * 32; base < np; base += nwarp * 32) {
     const int i = base + lane;
@@ -632,8 +637,8 @@ __global__ void __launch_bounds__(256)
       v.x = (double)a * is;
       v.y = (double)bb * is;
     } else {
-      v.x = dre[sidx];
-      v.y = dim_[sidx];
+      v.x = dre[sidx] * is;
+      v.y = dim_[sidx] * is;
     }
     const int64_t g = wrap_idx(G.org[0] + x, L.nf[0]) +
                       (int64_t)L.nf[0] * (wrap_idx(G.org[1] + y, L.nf[1]) +

@@ -131,7 +131,8 @@ def test_type3(oracle, dtype, dim, form):
     assert oracle.rel_l2(f, ref) < checktol
     same = oracle.nufft_es(3, _oracle_pts(pts), c, 1, tol, ss=_oracle_pts(freq),
                            is_float=dtype == "complex64", kernel=_kernel(plan))
-    assert oracle.rel_l2(f, same) < (3e-5 if dtype == "complex64" else 1e-9)
+    # (double: both sit at errors near tol on either side of the direct sum)
+    assert oracle.rel_l2(f, same) < (3e-5 if dtype == "complex64" else 3 * tol)
     if _kernel(plan) == "es":
         assert oracle.rel_l2(f, ref) < _bound(oracle.rel_l2(same, ref), dtype)
     else:

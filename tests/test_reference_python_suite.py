@@ -1,0 +1,36 @@
+"""The reference's own Python test suite (python/cufinufft/tests of
+flatironinstitute/finufft: test_basic, test_simple, test_multi and
+test_error_checks), run unchanged with its own binding against this library
+(the binding finds it through LD_LIBRARY_PATH, as a system install would be
+found), with torch as the array framework. The reference files are copied
+to baseline/_ref/cufinufft_py by oracle/Makefile target ref-py-src; the test
+is skipped where that copy is absent."""
+import os
+import subprocess
+import sys
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REFPY = os.path.join(ROOT, "baseline", "_ref", "cufinufft_py")
+LIB_DIR = os.path.join(ROOT, "finufft_gb300", "_build")
+
+
+@pytest.mark.parametrize("suite", ["test_basic.py", "test_simple.py", "test_multi.py",
+                                   "test_error_checks.py"])
+def test_reference_python_suite(suite):
+    path = os.path.join(REFPY, "tests", suite)
+    if not os.path.exists(path):
+        pytest.skip("reference Python suite not copied (oracle/Makefile ref-py-src)")
+    env = dict(os.environ, PYTHONPATH=REFPY + os.pathsep + os.path.join(REFPY, "tests"),
+               LD_LIBRARY_PATH=LIB_DIR + os.pathsep + os.environ.get("LD_LIBRARY_PATH", ""))
+    r = subprocess.run([sys.executable, "-m", "pytest", path, "--framework", "torch", "-q",
+                        "-p", "no:cacheprovider", "-x"],
+                       env=env, capture_output=True, text=True, cwd=os.path.join(REFPY, "tests"),
+                       timeout=1500)
+    tail = (r.stdout + r.stderr)[-3000:]
+    # exit 5: every test of the file skipped itself (test_multi needs two GPUs)
+    assert r.returncode in (0, 5), tail
+    assert "passed" in tail or r.returncode == 5, tail
