@@ -171,6 +171,8 @@ def _declare(lib):
     lib.gbnufft_planner_candidate.argtypes = [c_int, c_int, c_int, POINTER(c_double), ip, ip,
                                               ip, ip]
     lib.gbnufft_planner_candidate.restype = c_int
+    lib.gbnufft_planner_valid.argtypes = [c_int, c_int, c_int, c_double, c_int, ip]
+    lib.gbnufft_planner_valid.restype = c_int
     lib.gbnufft_planner_model.argtypes = [ip, c_void_p, c_void_p, c_void_p, c_void_p,
                                           c_void_p, fp, fp]
     lib.gbnufft_planner_model.restype = c_int

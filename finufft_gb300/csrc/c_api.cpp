@@ -355,6 +355,16 @@ int gbnufft_planner_candidate(int dim, int is_double, int slot, double *sigma, i
   });
 }
 
+int gbnufft_planner_valid(int type, int dim, int is_double, double tol, int slot, int *valid) {
+  return guarded([&] {
+    if (!valid) GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "valid");
+    gbn::Candidate c;
+    if (!gbn::planner_candidate(dim, is_double != 0, slot, &c))
+      GBN_THROW(FINUFFT_ERR_INVALID_ARGUMENT, "slot");
+    *valid = gbn::planner_candidate_valid(c, type, dim, is_double != 0, tol) ? 1 : 0;
+  });
+}
+
 int gbnufft_planner_model(int *trained, float *weights, float *mean, float *stdev, float *lo,
                           float *hi, float *ymean, float *ystd) {
   return guarded([&] {

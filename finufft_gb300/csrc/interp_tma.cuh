@@ -62,7 +62,7 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const void *map, int c
 
 // points per thread: the weights of PPT points stay in registers
 template <typename T, int DIM, int NS> __host__ __device__ constexpr int tma_ppt() {
-  return DIM * NS * (int)sizeof(T) / 4 <= 24 ? 4 : (DIM * NS * (int)sizeof(T) / 4 <= 48 ? 2 : 1);
+  return DIM * NS * (int)sizeof(T) / 4 <= 12 ? 4 : (DIM * NS * (int)sizeof(T) / 4 <= 24 ? 2 : 1);
 }
 
 template <typename T, int DIM, int NS>
@@ -118,10 +118,15 @@ __global__ void __launch_bounds__(INTERP_TMA_THREADS)
     else
       tma_load_4d(sbuf0 + s * buf_stride, &tmap, xs * xmul, G.org[1], G.org[2], k, bar[s]);
   };
-  for (int c0 = 0; c0 < np; c0 += PPT * (int)blockDim.x) {
-    T kx[PPT][NS], ky[PPT][NS], kz[PPT][DIM == 3 ? NS : 1];
-    int off[PPT], jj[PPT];
-    cplx<T> pf[PPT];
+  // weights of the thread's points of one chunk (PPT * blockDim points): kept
+  // across transforms when one chunk holds the subproblem, else recomputed per
+  // transform while the tile of that transform serves every chunk
+  const int per_chunk = PPT * (int)blockDim.x;
+  const bool one_chunk = np <= per_chunk;
+  T kx[PPT][NS], ky[PPT][NS], kz[PPT][DIM == 3 ? NS : 1];
+  int off[PPT], jj[PPT];
+  cplx<T> pf[PPT];
+  auto load_weights = [&](int c0) {
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
       const int i = c0 + threadIdx.x + q * (int)blockDim.x;
@@ -143,38 +148,42 @@ __global__ void __launch_bounds__(INTERP_TMA_THREADS)
         }
       }
     }
-    for (int k = 0; k < ntr; ++k) {
-      const int s = k & 1;
-      cplx<T> *buf = reinterpret_cast<cplx<T> *>(sm + s * buf_stride);
-      if (interior) {
-        if (threadIdx.x == 0) {
-          if (k == 0) issue(0);
-          if (k + 1 < ntr) issue(k + 1); // its buffer was released at the end of k - 1
-        }
-        if (!mbar_wait(bar[s], uses[s] & 1u)) {
-          // give up: flag it, wait (bounded) for this block's other copy, leave
-          if (threadIdx.x == 0) atomicExch(err, 1);
-          if (k + 1 < ntr) mbar_wait(bar[s ^ 1], uses[s ^ 1] & 1u);
-          return;
-        }
-        ++uses[s];
-      } else {
-        // boundary tile: per-thread loads with the periodic wrap, same layout
-        const cplx<T> *src = fw + (int64_t)k * nf_total;
-        const int rows = G.t[1] * (DIM == 3 ? G.t[2] : 1);
-        for (int r = threadIdx.x >> 5; r < rows; r += blockDim.x >> 5) {
-          const int y = r % G.t[1], z = r / G.t[1];
-          int64_t rb = (int64_t)L.nf[0] * wrap_idx(G.org[1] + y, L.nf[1]);
-          if constexpr (DIM == 3) rb += plane * wrap_idx(G.org[2] + z, L.nf[2]);
-          cplx<T> *dst = buf + (z * BY + y) * BX + xoff;
-          for (int x = threadIdx.x & 31; x < G.t[0]; x += 32)
-            dst[x] = src[rb + wrap_idx(G.org[0] + x, L.nf[0])];
-        }
-        __syncthreads();
+  };
+  if (one_chunk) load_weights(0);
+  for (int k = 0; k < ntr; ++k) {
+    const int s = k & 1;
+    cplx<T> *buf = reinterpret_cast<cplx<T> *>(sm + s * buf_stride);
+    if (interior) {
+      if (threadIdx.x == 0) {
+        if (k == 0) issue(0);
+        if (k + 1 < ntr) issue(k + 1); // its buffer was released at the end of k - 1
       }
-      const uint32_t sb = sbuf0 + s * buf_stride;
-      constexpr uint32_t CS = sizeof(cplx<T>);
-      const uint32_t rs = (uint32_t)BX * CS, ps = (uint32_t)(BX * BY) * CS;
+      if (!mbar_wait(bar[s], uses[s] & 1u)) {
+        // give up: flag it, wait (bounded) for this block's other copy, leave
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        if (k + 1 < ntr) mbar_wait(bar[s ^ 1], uses[s ^ 1] & 1u);
+        return;
+      }
+      ++uses[s];
+    } else {
+      // boundary tile: per-thread loads with the periodic wrap, same layout
+      const cplx<T> *src = fw + (int64_t)k * nf_total;
+      const int rows = G.t[1] * (DIM == 3 ? G.t[2] : 1);
+      for (int r = threadIdx.x >> 5; r < rows; r += blockDim.x >> 5) {
+        const int y = r % G.t[1], z = r / G.t[1];
+        int64_t rb = (int64_t)L.nf[0] * wrap_idx(G.org[1] + y, L.nf[1]);
+        if constexpr (DIM == 3) rb += plane * wrap_idx(G.org[2] + z, L.nf[2]);
+        cplx<T> *dst = buf + (z * BY + y) * BX + xoff;
+        for (int x = threadIdx.x & 31; x < G.t[0]; x += 32)
+          dst[x] = src[rb + wrap_idx(G.org[0] + x, L.nf[0])];
+      }
+      __syncthreads();
+    }
+    const uint32_t sb = sbuf0 + s * buf_stride;
+    constexpr uint32_t CS = sizeof(cplx<T>);
+    const uint32_t rs = (uint32_t)BX * CS, ps = (uint32_t)(BX * BY) * CS;
+    for (int c0 = 0; c0 < np; c0 += per_chunk) {
+      if (!one_chunk) load_weights(c0);
 #pragma unroll
       for (int q = 0; q < PPT; ++q) {
         if (off[q] < 0) continue;
@@ -219,8 +228,7 @@ __global__ void __launch_bounds__(INTERP_TMA_THREADS)
         else
           out[(int64_t)k * L.M + jj[q]] = r;
       }
-      __syncthreads(); // buffer s is free for the copy of transform k + 2
     }
+    __syncthreads(); // buffer s is free for the copy of transform k + 2
   }
 }
-

@@ -429,24 +429,7 @@ template <typename T> void Plan<T>::make_fseries() {
 
 // ---------------------------------------------------------- planners 2, 3 ----
 template <typename T> bool Plan<T>::candidate_valid(const Candidate &c) const {
-  // analytic rejection: the kernel width for tol at this sigma -- the larger of
-  // the PSWF width law and the GPU rule, as the plan would pick it -- must fit
-  // the precision's widest kernel (unclipped, the law's aliasing bound reaches
-  // tol). In single precision a sigma below 2 also needs tol >= 1e-5: the
-  // larger range of 1/phihat lifts the float rounding above the tolerance
-  // below that (the engine's own timing and error sweeps: 16% of the sigma-1.5
-  // float plans at tol < 1e-5 had errors above 2 tol, none at sigma 2).
-  const bool is_float = std::is_same_v<T, float>;
-  const double t = std::max(tol, is_float ? (double)FLT_EPSILON : DBL_EPSILON);
-  const double tolfac = 0.18 * std::pow(1.4, dim - 1) * (type == 3 ? 1.4 : 1.0);
-  const double u = PI * std::sqrt(1.0 - 1.0 / c.sigma);
-  const int ns_law = (int)std::ceil(std::log(tolfac / t) / u + 1.0);
-  const int ns_gpu = c.sigma == 2.0 ? (int)std::ceil(-std::log10(t / 10.0))
-                                    : (int)std::ceil(-std::log(t) / u);
-  const int ns = std::max(2, std::max(ns_law, ns_gpu));
-  const int maxns = is_float ? MAX_NS_FLOAT : MAX_NS;
-  if (is_float && c.sigma < 2.0 && tol < 1e-5) return false;
-  return ns <= maxns && kernel_tol_bound(ns, c.sigma, dim, type) <= t * (1 + 1e-9);
+  return planner_candidate_valid(c, type, dim, std::is_same_v<T, double>, tol);
 }
 
 template <typename T> void Plan<T>::apply_sigma(double sigma) {

@@ -12,6 +12,7 @@
 #include "planner.h"
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -59,6 +60,26 @@ bool planner_candidate(int dim, bool dbl, int k, Candidate *c) {
   if (r.reference) r.bins[0] = r.bins[1] = r.bins[2] = 0; // the heuristic's
   *c = r;
   return true;
+}
+
+bool planner_candidate_valid(const Candidate &c, int type, int dim, bool dbl, double tol) {
+  // analytic rejection: the kernel width for tol at this sigma -- the larger of
+  // the PSWF width law and the GPU rule, as the plan would pick it -- must fit
+  // the precision's widest kernel (unclipped, the law's aliasing bound reaches
+  // tol). In single precision a sigma below 2 also needs tol >= 1e-5: the
+  // larger range of 1/phihat lifts the float rounding above the tolerance
+  // below that (the engine's own timing and error sweeps: 16% of the sigma-1.5
+  // float plans at tol < 1e-5 had errors above 2 tol, none at sigma 2).
+  const double t = std::max(tol, dbl ? DBL_EPSILON : (double)FLT_EPSILON);
+  const double tolfac = 0.18 * std::pow(1.4, dim - 1) * (type == 3 ? 1.4 : 1.0);
+  const double u = PI * std::sqrt(1.0 - 1.0 / c.sigma);
+  const int ns_law = (int)std::ceil(std::log(tolfac / t) / u + 1.0);
+  const int ns_gpu = c.sigma == 2.0 ? (int)std::ceil(-std::log10(t / 10.0))
+                                    : (int)std::ceil(-std::log(t) / u);
+  const int ns = std::max(2, std::max(ns_law, ns_gpu));
+  const int maxns = dbl ? MAX_NS : MAX_NS_FLOAT;
+  if (!dbl && c.sigma < 2.0 && tol < 1e-5) return false;
+  return ns <= maxns && kernel_tol_bound(ns, c.sigma, dim, type) <= t * (1 + 1e-9);
 }
 
 double kernel_tol_bound(int ns, double sigma, int dim, int type) {

@@ -46,6 +46,9 @@ bool planner_candidate(int dim, bool dbl, int k, Candidate *c);
 // src/common/kernel.cpp:60-95): a candidate whose width had to be clipped
 // below the law's width for tol is rejected.
 double kernel_tol_bound(int ns, double sigma, int dim, int type);
+// Whether a plan of this type/dimension/precision at tol may take candidate c
+// (the analytic rejection of the learned planner and the autotuner).
+bool planner_candidate_valid(const Candidate &c, int type, int dim, bool dbl, double tol);
 
 // Raw features of a problem (see planner.cu for the list); the occupancy
 // statistics come from a coarse histogram of (a strided sample of) the points,

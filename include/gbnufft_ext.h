@@ -166,6 +166,11 @@ GBNUFFT_EXPORT int gbnufft_planner_dims(int *nfeat, int *hidden, int *nslots, in
 GBNUFFT_EXPORT int gbnufft_planner_candidate(int dim, int is_double, int slot, double *sigma,
                                              int *bins, int *maxsub, int *variant,
                                              int *reference);
+/* planner_valid: whether a plan of this type, dimension, precision and tol may
+ * take slot k (its kernel width at the slot's sigma fits unclipped; single
+ * precision takes sigma < 2 only at tol >= 1e-5). */
+GBNUFFT_EXPORT int gbnufft_planner_valid(int type, int dim, int is_double, double tol, int slot,
+                                         int *valid);
 GBNUFFT_EXPORT int gbnufft_planner_model(int *trained, float *weights, float *mean,
                                          float *stdev, float *lo, float *hi, float *ymean,
                                          float *ystd);

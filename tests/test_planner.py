@@ -218,3 +218,31 @@ def test_planned_transforms(oracle, planner, ty):
         assert info.planner_used == 3
         assert sum(v > 0 for v in info.tune_ms) >= 4
     assert oracle.rel_l2(got, ref) < 1.25 * oracle.rel_l2(same, ref) + 5e-6
+
+
+def test_candidate_rejection_rule(engine, oracle):
+    """the analytic rejection (CPU): a slot is valid when the kernel width the
+    plan would pick at the slot's sigma -- max(PSWF width law, GPU rule) --
+    fits the widest kernel of the precision; single precision takes sigma < 2
+    only at tol >= 1e-5"""
+    v = ctypes.c_int()
+    for dbl in (0, 1):
+        for dim in (2, 3):
+            for ty in (1, 2, 3):
+                for tol in (1e-2, 1e-4, 1e-5, 3e-6, 1e-6, 1e-8, 1e-10, 1e-12, 1e-14):
+                    for k in range(12):
+                        rc, c = _candidate(engine, dim, dbl, k)
+                        if rc:
+                            continue
+                        sigma = c[0]
+                        assert engine.gbnufft_planner_valid(ty, dim, dbl, tol, k,
+                                                            ctypes.byref(v)) == 0
+                        eps = max(tol, 2.2e-16 if dbl else 1.19e-7)
+                        law = oracle.cpu_kernel(eps, dim, ty, sigma, not dbl, clip=False)[0]
+                        u = math.pi * math.sqrt(1 - 1 / sigma)
+                        gpu = (math.ceil(-math.log10(eps / 10)) if sigma == 2.0
+                               else math.ceil(-math.log(eps) / u))
+                        want = max(law, gpu, 2) <= (16 if dbl else 12)
+                        if not dbl and sigma < 2 and tol < 1e-5:
+                            want = False
+                        assert v.value == int(want), (dbl, dim, ty, tol, k)
