@@ -1,3 +1,4 @@
+#include <algorithm>
 #include <limits>
 #include <map>
 #include <mutex>
@@ -149,12 +150,15 @@ __global__ void inv_fseries_kernel(int nf, QuadNodes Q, T *inv) {
   }
 }
 
-// Deconvolution and amplification walk rows along x: one block per chunk of
-// DC_X positions of one row (a row = fixed y, z and transform), so the row's
-// indices, its y/z factors and its grid row are found once per block with
-// 32-bit arithmetic, and the threads read and write contiguous x runs.
+// Deconvolution and amplification walk rows along x in warp items: a warp
+// takes DC_W consecutive x positions of one row (a row = fixed y, z and
+// transform), finds the row's indices, its y/z factor and its grid row once
+// with 32-bit arithmetic, and its lanes read and write contiguous x runs
+// (eight positions each); warps stride over the items.
 constexpr int DC_THREADS = 256;
-constexpr int DC_X = 1024; // x positions per block
+constexpr int DC_W = 256; // x positions per warp item
+
+__device__ __forceinline__ int dc_items(int len) { return (len + DC_W - 1) / DC_W; }
 
 // fk[t][k] = fw[t][wrap(k)] / (phihat_x(kx) phihat_y(ky) phihat_z(kz)) (type 1)
 template <typename T, int DIM>
@@ -162,40 +166,46 @@ __global__ void __launch_bounds__(DC_THREADS)
     deconv_kernel(int ms0, int ms1, int ms2, int nf0, int nf1, int nf2, int modeord,
                   const T *__restrict__ i0, const T *__restrict__ i1, const T *__restrict__ i2,
                   const cplx<T> *__restrict__ fw, int64_t nf_total, cplx<T> *__restrict__ fk,
-                  int64_t nmodes, int xchunks) {
-  const int row = blockIdx.x / xchunks;
-  const int x0 = (blockIdx.x - row * xchunks) * DC_X;
-  int iy = 0, iz = 0, tr = row;
-  if (DIM > 1) {
-    iy = row % ms1;
-    tr = row / ms1;
-  }
-  if (DIM > 2) {
-    iz = tr % ms2;
-    tr /= ms2;
-  }
-  T fyz = T(1);
-  int64_t grow = (int64_t)tr * nf_total;
-  if (DIM > 1) {
-    const int ky = mode_of(iy, ms1, modeord);
-    grow += (int64_t)nf0 * (ky >= 0 ? ky : nf1 + ky);
-    fyz = i1[ky >= 0 ? ky : -ky];
-  }
-  if (DIM > 2) {
-    const int kz = mode_of(iz, ms2, modeord);
-    grow += (int64_t)nf0 * nf1 * (kz >= 0 ? kz : nf2 + kz);
-    fyz *= i2[kz >= 0 ? kz : -kz];
-  }
-  const int64_t orow = (int64_t)tr * nmodes + (int64_t)ms0 * (iy + (int64_t)ms1 * iz);
-  const int x1 = min(ms0, x0 + DC_X);
-  for (int ix = x0 + threadIdx.x; ix < x1; ix += DC_THREADS) {
-    const int kx = mode_of(ix, ms0, modeord);
-    const cplx<T> v = fw[grow + (kx >= 0 ? kx : nf0 + kx)];
-    const T f = fyz * i0[kx >= 0 ? kx : -kx];
-    cplx<T> r;
-    r.x = v.x * f;
-    r.y = v.y * f;
-    fk[orow + ix] = r;
+                  int64_t nmodes, int64_t nitems) {
+  const int lane = threadIdx.x & 31;
+  const int xchunks = dc_items(ms0);
+  const int64_t wstride = (int64_t)gridDim.x * (DC_THREADS / 32);
+  for (int64_t it = (int64_t)blockIdx.x * (DC_THREADS / 32) + (threadIdx.x >> 5); it < nitems;
+       it += wstride) {
+    const int row = (int)(it / xchunks);
+    const int x0 = (int)(it - (int64_t)row * xchunks) * DC_W;
+    int iy = 0, iz = 0, tr = row;
+    if (DIM > 1) {
+      iy = tr % ms1;
+      tr /= ms1;
+    }
+    if (DIM > 2) {
+      iz = tr % ms2;
+      tr /= ms2;
+    }
+    T fyz = T(1);
+    int64_t grow = (int64_t)tr * nf_total;
+    if (DIM > 1) {
+      const int ky = mode_of(iy, ms1, modeord);
+      grow += (int64_t)nf0 * (ky >= 0 ? ky : nf1 + ky);
+      fyz = i1[ky >= 0 ? ky : -ky];
+    }
+    if (DIM > 2) {
+      const int kz = mode_of(iz, ms2, modeord);
+      grow += (int64_t)nf0 * nf1 * (kz >= 0 ? kz : nf2 + kz);
+      fyz *= i2[kz >= 0 ? kz : -kz];
+    }
+    const int64_t orow = (int64_t)tr * nmodes + (int64_t)ms0 * (iy + (int64_t)ms1 * iz);
+    const int x1 = min(ms0, x0 + DC_W);
+    for (int ix = x0 + lane; ix < x1; ix += 32) {
+      const int kx = mode_of(ix, ms0, modeord);
+      const cplx<T> v = fw[grow + (kx >= 0 ? kx : nf0 + kx)];
+      const T f = fyz * i0[kx >= 0 ? kx : -kx];
+      cplx<T> r;
+      r.x = v.x * f;
+      r.y = v.y * f;
+      fk[orow + ix] = r;
+    }
   }
 }
 
@@ -205,53 +215,59 @@ __global__ void __launch_bounds__(DC_THREADS)
     amplify_kernel(int ms0, int ms1, int ms2, int nf0, int nf1, int nf2, int modeord,
                    const T *__restrict__ i0, const T *__restrict__ i1, const T *__restrict__ i2,
                    const cplx<T> *__restrict__ fk, int64_t nmodes, cplx<T> *__restrict__ fw,
-                   int64_t nf_total, int xchunks) {
-  const int row = blockIdx.x / xchunks;
-  const int x0 = (blockIdx.x - row * xchunks) * DC_X;
-  int gy = 0, gz = 0, tr = row;
-  if (DIM > 1) {
-    gy = row % nf1;
-    tr = row / nf1;
-  }
-  if (DIM > 2) {
-    gz = tr % nf2;
-    tr /= nf2;
-  }
-  bool in = true;
-  T fyz = T(1);
-  int64_t irow = (int64_t)tr * nmodes;
-  if (DIM > 1) {
-    const int ky = gy <= (ms1 - 1) / 2 ? gy : (gy >= nf1 - ms1 / 2 ? gy - nf1 : INT32_MIN);
-    in = ky != INT32_MIN;
-    if (in) {
-      irow += (int64_t)ms0 * pos_of(ky, ms1, modeord);
-      fyz = i1[ky >= 0 ? ky : -ky];
+                   int64_t nf_total, int64_t nitems) {
+  const int lane = threadIdx.x & 31;
+  const int xchunks = dc_items(nf0);
+  const int64_t wstride = (int64_t)gridDim.x * (DC_THREADS / 32);
+  for (int64_t it = (int64_t)blockIdx.x * (DC_THREADS / 32) + (threadIdx.x >> 5); it < nitems;
+       it += wstride) {
+    const int row = (int)(it / xchunks);
+    const int x0 = (int)(it - (int64_t)row * xchunks) * DC_W;
+    int gy = 0, gz = 0, tr = row;
+    if (DIM > 1) {
+      gy = tr % nf1;
+      tr /= nf1;
     }
-  }
-  if (DIM > 2 && in) {
-    const int kz = gz <= (ms2 - 1) / 2 ? gz : (gz >= nf2 - ms2 / 2 ? gz - nf2 : INT32_MIN);
-    in = kz != INT32_MIN;
-    if (in) {
-      irow += (int64_t)ms0 * ms1 * pos_of(kz, ms2, modeord);
-      fyz *= i2[kz >= 0 ? kz : -kz];
+    if (DIM > 2) {
+      gz = tr % nf2;
+      tr /= nf2;
     }
-  }
-  const int64_t grow = (int64_t)tr * nf_total + (int64_t)nf0 * (gy + (int64_t)nf1 * gz);
-  const int x1 = min(nf0, x0 + DC_X);
-  for (int gx = x0 + threadIdx.x; gx < x1; gx += DC_THREADS) {
-    cplx<T> r;
-    r.x = T(0);
-    r.y = T(0);
-    if (in) {
-      const int kx = gx <= (ms0 - 1) / 2 ? gx : (gx >= nf0 - ms0 / 2 ? gx - nf0 : INT32_MIN);
-      if (kx != INT32_MIN) {
-        const cplx<T> v = fk[irow + pos_of(kx, ms0, modeord)];
-        const T f = fyz * i0[kx >= 0 ? kx : -kx];
-        r.x = v.x * f;
-        r.y = v.y * f;
+    bool in = true;
+    T fyz = T(1);
+    int64_t irow = (int64_t)tr * nmodes;
+    if (DIM > 1) {
+      const int ky = gy <= (ms1 - 1) / 2 ? gy : (gy >= nf1 - ms1 / 2 ? gy - nf1 : INT32_MIN);
+      in = ky != INT32_MIN;
+      if (in) {
+        irow += (int64_t)ms0 * pos_of(ky, ms1, modeord);
+        fyz = i1[ky >= 0 ? ky : -ky];
       }
     }
-    fw[grow + gx] = r;
+    if (DIM > 2 && in) {
+      const int kz = gz <= (ms2 - 1) / 2 ? gz : (gz >= nf2 - ms2 / 2 ? gz - nf2 : INT32_MIN);
+      in = kz != INT32_MIN;
+      if (in) {
+        irow += (int64_t)ms0 * ms1 * pos_of(kz, ms2, modeord);
+        fyz *= i2[kz >= 0 ? kz : -kz];
+      }
+    }
+    const int64_t grow = (int64_t)tr * nf_total + (int64_t)nf0 * (gy + (int64_t)nf1 * gz);
+    const int x1 = min(nf0, x0 + DC_W);
+    for (int gx = x0 + lane; gx < x1; gx += 32) {
+      cplx<T> r;
+      r.x = T(0);
+      r.y = T(0);
+      if (in) {
+        const int kx = gx <= (ms0 - 1) / 2 ? gx : (gx >= nf0 - ms0 / 2 ? gx - nf0 : INT32_MIN);
+        if (kx != INT32_MIN) {
+          const cplx<T> v = fk[irow + pos_of(kx, ms0, modeord)];
+          const T f = fyz * i0[kx >= 0 ? kx : -kx];
+          r.x = v.x * f;
+          r.y = v.y * f;
+        }
+      }
+      fw[grow + gx] = r;
+    }
   }
 }
 
@@ -333,28 +349,34 @@ template <typename T> void launch_inv_fseries(int nf, const QuadNodes &Q, T *inv
   GBN_LAUNCH_CHECK();
 }
 
+// warp items of a row walk: rows x ceil(len / DC_W); blocks of 8 warps, at
+// most 16 per SM (they stride over the items)
+inline unsigned dc_blocks(int64_t nitems) {
+  const int64_t want = (nitems + DC_THREADS / 32 - 1) / (DC_THREADS / 32);
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, 152 * 16));
+}
+
 template <typename T>
 void launch_deconv(int dim, const int ms[3], const int nf[3], int modeord, const T *const inv[3],
                    const cplx<T> *fw, int64_t nf_total, cplx<T> *fk, int ntr, cudaStream_t s) {
   const int64_t nmodes = (int64_t)ms[0] * ms[1] * ms[2];
-  const int xchunks = (ms[0] + DC_X - 1) / DC_X;
-  const int64_t blocks = (int64_t)xchunks * ms[1] * ms[2] * ntr;
-  if (blocks <= 0) return;
-  if (blocks > std::numeric_limits<int32_t>::max())
-    GBN_THROW(FINUFFT_ERR_MAXNALLOC, "deconvolution grid");
-  const unsigned g = (unsigned)blocks;
+  const int64_t nitems = (int64_t)((ms[0] + DC_W - 1) / DC_W) * ms[1] * ms[2] * ntr;
+  if (nitems <= 0) return;
+  if ((int64_t)ms[1] * ms[2] * ntr > std::numeric_limits<int32_t>::max())
+    GBN_THROW(FINUFFT_ERR_MAXNALLOC, "deconvolution rows");
+  const unsigned g = dc_blocks(nitems);
   if (dim == 1)
     deconv_kernel<T, 1><<<g, DC_THREADS, 0, s>>>(ms[0], 1, 1, nf[0], 1, 1, modeord, inv[0],
                                                  inv[0], inv[0], fw, nf_total, fk, nmodes,
-                                                 xchunks);
+                                                 nitems);
   else if (dim == 2)
     deconv_kernel<T, 2><<<g, DC_THREADS, 0, s>>>(ms[0], ms[1], 1, nf[0], nf[1], 1, modeord,
                                                  inv[0], inv[1], inv[1], fw, nf_total, fk,
-                                                 nmodes, xchunks);
+                                                 nmodes, nitems);
   else
     deconv_kernel<T, 3><<<g, DC_THREADS, 0, s>>>(ms[0], ms[1], ms[2], nf[0], nf[1], nf[2],
                                                  modeord, inv[0], inv[1], inv[2], fw, nf_total,
-                                                 fk, nmodes, xchunks);
+                                                 fk, nmodes, nitems);
   GBN_LAUNCH_CHECK();
 }
 
@@ -363,24 +385,23 @@ void launch_amplify(int dim, const int ms[3], const int nf[3], int modeord,
                     const T *const inv[3], const cplx<T> *fk, cplx<T> *fw, int64_t nf_total,
                     int ntr, cudaStream_t s) {
   const int64_t nmodes = (int64_t)ms[0] * ms[1] * ms[2];
-  const int xchunks = (nf[0] + DC_X - 1) / DC_X;
-  const int64_t blocks = (int64_t)xchunks * nf[1] * nf[2] * ntr;
-  if (blocks <= 0) return;
-  if (blocks > std::numeric_limits<int32_t>::max())
-    GBN_THROW(FINUFFT_ERR_MAXNALLOC, "amplification grid");
-  const unsigned g = (unsigned)blocks;
+  const int64_t nitems = (int64_t)((nf[0] + DC_W - 1) / DC_W) * nf[1] * nf[2] * ntr;
+  if (nitems <= 0) return;
+  if ((int64_t)nf[1] * nf[2] * ntr > std::numeric_limits<int32_t>::max())
+    GBN_THROW(FINUFFT_ERR_MAXNALLOC, "amplification rows");
+  const unsigned g = dc_blocks(nitems);
   if (dim == 1)
     amplify_kernel<T, 1><<<g, DC_THREADS, 0, s>>>(ms[0], 1, 1, nf[0], 1, 1, modeord, inv[0],
                                                   inv[0], inv[0], fk, nmodes, fw, nf_total,
-                                                  xchunks);
+                                                  nitems);
   else if (dim == 2)
     amplify_kernel<T, 2><<<g, DC_THREADS, 0, s>>>(ms[0], ms[1], 1, nf[0], nf[1], 1, modeord,
                                                   inv[0], inv[1], inv[1], fk, nmodes, fw,
-                                                  nf_total, xchunks);
+                                                  nf_total, nitems);
   else
     amplify_kernel<T, 3><<<g, DC_THREADS, 0, s>>>(ms[0], ms[1], ms[2], nf[0], nf[1], nf[2],
                                                   modeord, inv[0], inv[1], inv[2], fk, nmodes,
-                                                  fw, nf_total, xchunks);
+                                                  fw, nf_total, nitems);
   GBN_LAUNCH_CHECK();
 }
 

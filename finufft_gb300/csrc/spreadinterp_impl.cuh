@@ -454,8 +454,41 @@ __device__ __forceinline__ dfloat df_mul(dfloat a, dfloat b) {
   const float h = p + e;
   return {h, e - (h - p)};
 }
+// round(f) as int64 for |f| < 2^63 from the float's bits, on the integer
+// pipes: a 64-bit float-to-integer conversion instruction runs on the FP64
+// pipe, which GB300 issues at a small fraction of its integer rate (ncu on the
+// FP64 spread: that pipe 34% busy and the kernel bound by it with
+// __float2ll_rn). Ties round away from zero; magnitudes below 1/2 give 0.
+__device__ __forceinline__ long long f2ll_bits(float f) {
+  const unsigned b = __float_as_uint(f);
+  const int e = (int)((b >> 23) & 255u); // biased exponent: |f| = m 2^(e - 150)
+  const long long m = (long long)((b & 0x7fffffu) | 0x800000u);
+  const int sh = e - 150;
+  long long v;
+  if (sh >= 0) v = m << sh;                                     // integral (|f| >= 2^23)
+  else if (sh > -25) v = (m + (1ll << (-sh - 1))) >> (-sh);     // round half away
+  else v = 0;                                                   // |f| < 2^-1, zero, subnormal
+  return (b >> 31) ? -v : v;
+}
 __device__ __forceinline__ long long df_to_ll(dfloat a) {
-  return __float2ll_rn(a.h) + __float2ll_rn(a.l);
+  return f2ll_bits(a.h) + f2ll_bits(a.l);
+}
+// v * 2^-e as a double, assembled from the integer's bits (integer pipes, see
+// f2ll_bits), rounded to nearest (ties away); |v| < 2^63, 2^-e a normal double
+__device__ __forceinline__ double ll_scaled(long long v, int e) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
+  unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+  const int lz = __clzll(a);
+  a <<= lz;                                        // leading one at bit 63
+  unsigned long long mant = (a >> 11) + ((a >> 10) & 1ull); // 53 bits, rounded
+  long long ex = 1023 + (63 - lz) - e;
+  if (mant >> 53) { // the rounding carried into a new bit
+    mant >>= 1;
+    ++ex;
+  }
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) |
+                                          (mant & ((1ull << 52) - 1))));
 }
 
 template <int NS>
@@ -468,6 +501,7 @@ __global__ void __launch_bounds__(256)
   __shared__ int mode; // 0: fixed point, 1: double atomics
   __shared__ double inv_scale;
   __shared__ double scale_d;
+  __shared__ int scale_e;
   constexpr int SK = STAGE_STRIDE;
   constexpr int NXB = (NS + 7) / 8;
   constexpr int NPAIR = NS * NS;
@@ -538,6 +572,7 @@ __global__ void __launch_bounds__(256)
     }
     scale_d = ldexp(1.0, e);
     inv_scale = ldexp(1.0, -e);
+    scale_e = e;
   }
   __syncthreads();
   const bool fx = mode == 0;
@@ -625,6 +660,7 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   double2 *fwt = fw + (int64_t)tr * nf_total + goff;
   const double is = inv_scale;
+  const int se = scale_e;
   for (int q = threadIdx.x; q < G.cells; q += blockDim.x) {
     const int x = q % G.t[0];
     const int y = (q / G.t[0]) % G.t[1];
@@ -634,8 +670,8 @@ __global__ void __launch_bounds__(256)
     if (fx) {
       const long long a = ire[sidx], bb = iim[sidx];
       if ((a | bb) == 0) continue;
-      v.x = (double)a * is;
-      v.y = (double)bb * is;
+      v.x = ll_scaled(a, se);
+      v.y = ll_scaled(bb, se);
     } else {
       v.x = dre[sidx] * is;
       v.y = dim_[sidx] * is;
@@ -2012,9 +2048,11 @@ template <typename T, int DIM> struct Dispatch {
         const int BX = (t0 + 2) & ~1; // even, at least t0 + 1
         const int xm = sizeof(T) == 8 ? 2 : 1;
         const size_t box = (size_t)BX * t1 * t2 * sizeof(cplx<T>);
-        const size_t smem = 2 * ((box + 127) / 128 * 128) + 128; // + alignment slack
+        // one buffer for a single transform (no copy to overlap: more blocks per
+        // SM), two otherwise; + alignment slack
+        const size_t smem = (ntr > 1 ? 2 : 1) * ((box + 127) / 128 * 128) + 128;
         CUtensorMap map;
-        if (BX * xm <= 256 && t1 <= 256 && t2 <= 256 && BX <= L.nf[0] && smem <= 100 * 1024 &&
+        if (BX * xm <= 256 && t1 <= 256 && t2 <= 256 && BX <= L.nf[0] && smem <= 112 * 1024 &&
             encode_grid_map<T>(&map, fw, DIM, L.nf, ntr, BX, t1, t2)) {
           auto kt = interp_tma_kernel<T, DIM, NS>;
           GBN_CUDA(cudaFuncSetAttribute(kt, cudaFuncAttributeMaxDynamicSharedMemorySize,
