@@ -324,7 +324,10 @@ def run_gpu(args):
     # plain GPU form: one transform, the reference library's heuristic planning
     plain_kw = dict(plan_kw)
     plain_kw["planner"] = 1
-    ms_plain, st_plain, info_plain, _, f_plain = single(plain_kw)
+    if args.only == "batched":
+        ms_plain = st_plain = info_plain = f_plain = None
+    else:
+        ms_plain, st_plain, info_plain, _, f_plain = single(plain_kw)
     if args.only == "plain":
         print(json.dumps({"plain_ms": ms_plain, "stage_ms": st_plain, "M": M,
                           "nsub": info_plain.nsub, "bins": list(info_plain.bins)}))
@@ -332,7 +335,8 @@ def run_gpu(args):
     # this engine's fixed default planning (planner 0), one transform
     eng_kw = dict(plan_kw)
     eng_kw["planner"] = 0
-    ms_eng, st_eng, info_eng, setpts_s, f_eng = single(eng_kw)
+    if args.only != "batched":
+        ms_eng, st_eng, info_eng, setpts_s, f_eng = single(eng_kw)
     if args.only == "engine":
         print(json.dumps({"engine_ms": ms_eng, "stage_ms": st_eng, "M": M,
                           "nsub": info_eng.nsub, "bins": list(info_eng.bins)}))
@@ -362,6 +366,10 @@ def run_gpu(args):
     torch.cuda.synchronize()
     stb = bplan.stage_times(True)
     binfo = bplan.info()
+    if args.only == "batched":
+        print(json.dumps({"batched_ms": ms_batched, "stage_ms": stb, "M": M, "ntransf": nt,
+                          "nsub": binfo.nsub, "bins": list(binfo.bins)}))
+        return
 
     # e2e through the reference-facing host-pointer C ABI (finufftf_makeplan /
     # setpts / execute) with pinned host arrays: every step copies the nt strength
@@ -841,7 +849,8 @@ def cfg_c3f64(args, dev, stream, with_cpu=True):
     gd = torch.Generator(device="cuda").manual_seed(99)
     c = torch.randn(M, 2, generator=gd, device="cuda", dtype=torch.float64).view(torch.complex128)[:, 0]
     x, y, z = (pts[d].contiguous() for d in range(3))
-    p = fg.Plan(1, N_MODES, eps=1e-12, dtype="complex128", gpu_stream=stream.cuda_stream)
+    kw = {"spread_variant": args.variant} if args.variant >= 0 else {}
+    p = fg.Plan(1, N_MODES, eps=1e-12, dtype="complex128", gpu_stream=stream.cuda_stream, **kw)
     p.setpts(x, y, z)
     f = torch.empty(N_MODES, dtype=torch.complex128, device=dev)
     ms = time_steps(lambda: p.execute(c, out=f), stream, min(args.steps, 3), min(args.warmup, 1))
@@ -887,7 +896,8 @@ def cfg_c3t2(args, dev, stream, with_cpu=True):
     pts = clustered_points(M, 1234 + 3, rng_dev="cuda")
     g = torch.Generator(device="cuda").manual_seed(18)
     fk = torch.randn(*N_MODES, 2, generator=g, device="cuda").view(torch.complex64)[..., 0]
-    p = fg.Plan(2, N_MODES, eps=TOL, isign=-1, gpu_stream=stream.cuda_stream)
+    p = fg.Plan(2, N_MODES, eps=TOL, isign=-1, gpu_stream=stream.cuda_stream,
+                interp_mode=args.interp_mode)
     p.setpts(pts[0].contiguous(), pts[1].contiguous(), pts[2].contiguous())
     cc = torch.empty(M, dtype=torch.complex64, device=dev)
     ms = time_steps(lambda: p.execute(fk, out=cc), stream, args.steps, args.warmup)
@@ -908,6 +918,9 @@ def run_config(args):
     """One secondary configuration as its own JSON line (not the metric line)."""
     import torch
 
+    global N_MODES
+    if args.nmodes:  # smaller grids for profiling runs of c3f64 / c3t2
+        N_MODES = (args.nmodes,) * 3
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=dev)
     out = {"config_name": args.config, "n_gpus": 1, "data": "synthetic (seeded)"}
@@ -981,10 +994,14 @@ def main():
     ap.add_argument("--bins", default="", help="bin sizes x,y,z (default: the planner's)")
     ap.add_argument("--maxsub", type=int, default=0, help="max points per subproblem")
     ap.add_argument("--variant", type=int, default=-1, help="3D spread variant (tuning runs)")
+    ap.add_argument("--interp-mode", type=int, default=0,
+                    help="type-2 interpolation schedule of --config c3t2 (0 auto, 1 gather, "
+                         "2 block tiles, 3 TMA tiles)")
     ap.add_argument("--planner", type=int, default=2,
                     help="planner of the planned forms (2 learned, 3 autotuned, 0 fixed default)")
-    ap.add_argument("--only", default="", choices=["", "plain", "engine"],
-                    help="time only the single-transform plan of that form (profiling runs)")
+    ap.add_argument("--only", default="", choices=["", "plain", "engine", "batched"],
+                    help="time only one form (profiling runs): a single-transform plan "
+                         "(plain, engine) or the batched plan")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -56,8 +56,8 @@ template <typename T> size_t spread_output_driven_bytes(int dim, int ns, const i
 template size_t spread_output_driven_bytes<float>(int, int, const int[3]);
 template size_t spread_output_driven_bytes<double>(int, int, const int[3]);
 
-size_t spread_tile3x_bytes(int ns, const int bin[3], int warps) {
-  return tile3_bytes<double>(ns, bin[0], bin[1], bin[2]) + (size_t)warps * t3x_stage_bytes(ns);
+size_t spread_tile3x_bytes(int ns, const int bin[3]) {
+  return t3x_bytes(ns, bin[0], bin[1], bin[2]);
 }
 template size_t spread_tile2m_bytes<float>(int, const int[3], int);
 template size_t spread_tile2m_bytes<double>(int, const int[3], int);

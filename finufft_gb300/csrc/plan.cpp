@@ -287,26 +287,18 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
     // default: 3 where its accumulators fit the register budget without spills
     // (single precision ns <= 8, double ns <= 5), else 2 for ns <= 8, else 0
     // double precision above that: 4, the int64 fixed-point tile summed with
-    // double-float products (no FP64 in the per-cell work)
+    // integer products (no FP64 in the per-cell work)
     const bool dbl = std::is_same_v<T, double>;
     const bool v3ok = !dbl ? ns <= 8 : ns <= 5;
     int variant = ext.planner == 1 ? 0 : (v3ok ? 3 : (dbl ? 4 : (ns <= 8 ? 2 : 0)));
     if (ext.spread_variant >= 0) variant = ext.spread_variant;
     if (variant == 1 && wsm > (size_t)limit) variant = 2;
     if (variant == 4 && dbl) {
-      // as many warps (up to 8) as fit beside the tile; two blocks per SM when
-      // half the shared memory holds the tile and four warps
-      const int half = 113 * 1024;
-      int w = 8;
-      while (w > 4 && spread_tile3x_bytes(ns, bins, w) > (size_t)half) --w;
-      if (spread_tile3x_bytes(ns, bins, w) > (size_t)half) {
-        w = 8;
-        while (w > 1 && spread_tile3x_bytes(ns, bins, w) > (size_t)limit) --w;
-      }
-      const size_t xsm = spread_tile3x_bytes(ns, bins, w);
+      // one block of 16 warps per SM sharing the tile and the staging buffers
+      const size_t xsm = spread_tile3x_bytes(ns, bins);
       if (xsm <= (size_t)limit) {
         S.cfg.variant = 4;
-        S.cfg.threads = 32 * w;
+        S.cfg.threads = 512;
         S.cfg.smem = xsm;
         S.smem = xsm;
         return S;

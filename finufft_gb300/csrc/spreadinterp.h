@@ -25,7 +25,7 @@ template <typename T> size_t spread_tile3m_bytes(int ns, const int bin[3], int w
 // Shared-memory bytes of the output-driven spread (method 3).
 template <typename T> size_t spread_output_driven_bytes(int dim, int ns, const int bin[3]);
 // Shared-memory bytes of the double-precision int64 fixed-point 3D spread (variant 4).
-size_t spread_tile3x_bytes(int ns, const int bin[3], int warps);
+size_t spread_tile3x_bytes(int ns, const int bin[3]);
 
 // A device word (one per device, allocated at first use) where kernels whose
 // bounded waits give up record it; device_error_take reads and clears it.

@@ -422,90 +422,64 @@ __global__ void __launch_bounds__(256)
 }
 
 // ---------------------------------------------------------------------------
-// Method 2 in 3D, double precision: variant 4, an int64 fixed-point tile.
-// GB300 issues FP64 at a small fraction of its FP32 rate, and shared-memory
-// double atomics are compare-and-swap loops around an FP64 add, so the double
-// spread (2 ns^3 updates per point, 4394 at ns = 13) was bound by FP64 issue.
-// Here each block first sums S = sum_j (|Re c_j| + |Im c_j|) over its
-// subproblem; a tile cell's sum is at most S (kernel values are at most 1;
-// margin 1.01), so the tile holds round(value * 2^e) in int64 with the power
-// of two 2^e <= 2^62 / (1.01 S), added by native 64-bit integer atomics. The
-// per-cell products are formed in double-float arithmetic (hi + lo float
-// pairs, ~46 significant bits, fused multiply-adds on the FP32 pipe) from the
-// FP64 kernel weights and strengths staged per point, and converted to int64
-// as round(hi) + round(lo). The integer sums are exact; each contribution is
-// rounded to S 2^-62 and carries the float pair's relative error (~2^-45),
-// far below the double-precision tolerances (the kernel is used at ns >= 6).
-// Subproblems whose S is not finite, or so small that 2^e would overflow,
-// sum doubles in the same tile with compare-and-swap atomics instead.
-// Staging and lane mapping follow spread_tile3_kernel.
-struct dfloat {
-  float h, l;
-};
-__device__ __forceinline__ dfloat df_from(double a) {
-  const float h = __double2float_rn(a);
-  return {h, __double2float_rn(a - (double)h)};
+// Method 2 in 3D, double precision: variant 4, an int64 fixed-point tile with
+// integer products. GB300 issues FP64 at a small fraction of its integer and
+// FP32 rates, and shared-memory double atomics are compare-and-swap loops
+// around an FP64 add, so a double spread that forms and adds its 2 ns^3
+// per-point updates (4394 at ns = 13) in FP64 is bound by the FP64 pipe.
+// Here the per-cell work is integer only:
+//  - each block sums S = sum_j (|Re c_j| + |Im c_j|) over its subproblem; a
+//    tile cell's sum is at most S (kernel values are at most 1; margin 1.01),
+//    so the tile holds round(value * 2^e) in int64 with 2^e <= 2^62 / (1.01 S),
+//    summed by native 64-bit integer shared-memory adds;
+//  - per point (FP64, ~3 ns Horner evaluations): U_z = round(c 2^e phi_z) as
+//    int64 and the y and x weights as 62-bit fractions W = round(phi 2^62);
+//  - per (y, z) row of the support a lane forms U_zy = U_z W_y / 2^64 and per
+//    cell U_zy W_x / 2^64, each from three 32 x 32-bit integer multiplies
+//    (mulfix below); the tile then holds sums of c phi 2^(e-4).
+// Each contribution carries the double products' relative error (2^-53) plus
+// a few units of S 2^-58 from the truncated products: double-precision
+// accuracy. Subproblems whose S is not finite or needs 2^e beyond 2^1000 sum
+// doubles (strengths scaled by a power of two) in the same tile instead.
+// The block's threads each own one (y, z) row of the support for a range of
+// the subproblem's points and sum it in registers over runs of points that
+// share their start cells; staged points come in two alternating buffers, so
+// the next points' FP64 weights are computed while the current ones are added.
+
+// u W / 2^64 for |u| <= 2^62 and W = wh 2^32 + wl (0 <= wh <= 2^30 + 1, wl
+// unsigned): uh wh + hi(uh wl) + hi(ul wh) + 1 from one wide and two high
+// 32-bit multiplies (hi: the high word of a 32 x 32-bit product; uh signed, so
+// hi(uh wl) = hi of the unsigned product minus wl when uh < 0). The high words
+// floor and the dropped ul wl / 2^64 lies in [0, 1); the constant 1 centres
+// the error (exact-integer emulation: |error| < 2 units, mean -0.06 units)
+__device__ __forceinline__ long long mulfix(long long u, int wh, unsigned wl) {
+  const int uh = (int)(u >> 32);
+  const unsigned ul = (unsigned)u;
+  const unsigned neg = (unsigned)(uh >> 31);
+  const long long t1 = (long long)uh * wh;
+  const int t2 = (int)(__umulhi((unsigned)uh, wl) - (wl & neg));
+  const unsigned t3 = __umulhi(ul, (unsigned)wh);
+  return t1 + (long long)t2 + (long long)t3 + 1;
 }
-__device__ __forceinline__ dfloat df_mul(dfloat a, dfloat b) {
-  const float p = a.h * b.h;
-  float e = fmaf(a.h, b.h, -p); // the product's rounding error, exactly
-  e = fmaf(a.h, b.l, e);
-  e = fmaf(a.l, b.h, e);
-  const float h = p + e;
-  return {h, e - (h - p)};
-}
-// round(f) as int64 for |f| < 2^63 from the float's bits, on the integer
-// pipes: a 64-bit float-to-integer conversion instruction runs on the FP64
-// pipe, which GB300 issues at a small fraction of its integer rate (ncu on the
-// FP64 spread: that pipe 34% busy and the kernel bound by it with
-// __float2ll_rn). Ties round away from zero; magnitudes below 1/2 give 0.
-__device__ __forceinline__ long long f2ll_bits(float f) {
-  const unsigned b = __float_as_uint(f);
-  const int e = (int)((b >> 23) & 255u); // biased exponent: |f| = m 2^(e - 150)
-  const long long m = (long long)((b & 0x7fffffu) | 0x800000u);
-  const int sh = e - 150;
-  long long v;
-  if (sh >= 0) v = m << sh;                                     // integral (|f| >= 2^23)
-  else if (sh > -25) v = (m + (1ll << (-sh - 1))) >> (-sh);     // round half away
-  else v = 0;                                                   // |f| < 2^-1, zero, subnormal
-  return (b >> 31) ? -v : v;
-}
-__device__ __forceinline__ long long df_to_ll(dfloat a) {
-  return f2ll_bits(a.h) + f2ll_bits(a.l);
-}
-// v * 2^-e as a double, assembled from the integer's bits (integer pipes, see
-// f2ll_bits), rounded to nearest (ties away); |v| < 2^63, 2^-e a normal double
-__device__ __forceinline__ double ll_scaled(long long v, int e) {
-  if (v == 0) return 0.0;
-  const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
-  unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
-  const int lz = __clzll(a);
-  a <<= lz;                                        // leading one at bit 63
-  unsigned long long mant = (a >> 11) + ((a >> 10) & 1ull); // 53 bits, rounded
-  long long ex = 1023 + (63 - lz) - e;
-  if (mant >> 53) { // the rounding carried into a new bit
-    mant >>= 1;
-    ++ex;
-  }
-  return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) |
-                                          (mant & ((1ull << 52) - 1))));
+// a weight as the (wh, wl) words of round(w 2^62); fitted kernel values can
+// dip a few ulps below zero at the support's edge, and are clamped to 0
+__device__ __forceinline__ int2 wfix(double w) {
+  const long long v = __double2ll_rn(fmax(w, 0.0) * 0x1p62);
+  return make_int2((int)(v >> 32), (int)(unsigned)v);
 }
 
 template <int NS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512, 1)
     spread_tile3x_kernel(PointLayout<double> L0, KernelShape<double> K,
                          const double2 *__restrict__ c, const double2 *__restrict__ pre,
                          int conj_pre, double2 *__restrict__ fw, int64_t nf_total) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double red[8];
-  __shared__ int mode; // 0: fixed point, 1: double atomics
-  __shared__ double inv_scale;
-  __shared__ double scale_d;
-  __shared__ int scale_e;
-  constexpr int SK = STAGE_STRIDE;
-  constexpr int NXB = (NS + 7) / 8;
+  __shared__ double red[16];
+  __shared__ int mode; // 0: fixed point, 1: double atomics, 2: all strengths zero
+  __shared__ double scale_d, inv_scale;
+  constexpr int SB = t3x_sb(NS);
+  constexpr int PS = t3x_point_bytes(NS);
   constexpr int NPAIR = NS * NS;
-  constexpr int NROUND = (NPAIR + 3) / 4;
   const int sub = blockIdx.x;
   const int tr = blockIdx.y;
   int b = L0.sub_bin[sub];
@@ -514,28 +488,16 @@ __global__ void __launch_bounds__(256)
   const PointLayout<double> &L = Lg;
   const int p0 = L.sub_start[sub];
   const int np = L.sub_count[sub];
+  if (np <= 0) return;
   const TileGeom<3> G = tile_of<double, 3, NS>(L, b);
-  const int px = tile_pitch_x(3, G.t[0]);
-  const int py = tile3_py(G.t[1], NS);
+  const int px = G.t[0], py = G.t[1];
   const int Q = px * py;
   const int ncell = Q * G.t[2];
   long long *ire = reinterpret_cast<long long *>(smem_raw);
   long long *iim = ire + ncell;
   double *dre = reinterpret_cast<double *>(ire), *dim_ = reinterpret_cast<double *>(iim);
+  unsigned char *stg0 = smem_raw + t3x_tile_bytes(ncell);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  unsigned char *stage = smem_raw + tile3_bytes<double>(NS, L.bin[0], L.bin[1], L.bin[2]) +
-                         (size_t)warp * t3x_stage_bytes(NS);
-  float *kxh = reinterpret_cast<float *>(stage);
-  float *kxl = kxh + NS * SK;
-  float *kyh = kxl + NS * SK;
-  float *kyl = kyh + NS * SK;
-  float *kzh = kyl + NS * SK;
-  float *kzl = kzh + NS * SK;
-  float *vrh = kzl + NS * SK;
-  float *vrl = vrh + SK;
-  float *vih = vrl + SK;
-  float *vil = vih + SK;
-  int *spk = reinterpret_cast<int *>(vil + SK);
   const double2 *ct = c + (int64_t)tr * L.M;
   // the subproblem's strength sum S, and the tile's scale
   double part = 0.0;
@@ -548,119 +510,172 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
   if (lane == 0) red[warp] = part;
-  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
-    ire[i] = 0;
-    iim[i] = 0;
+  {
+    uint4 *z4 = reinterpret_cast<uint4 *>(smem_raw);
+    const uint4 zero = make_uint4(0, 0, 0, 0);
+    for (int i = threadIdx.x; i < ncell; i += blockDim.x) { // 2 ncell int64 = ncell uint4
+      z4[i] = zero;
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     double S = 0.0;
     for (int w = 0; w < nwarp; ++w) S += red[w];
-    int e = 0;
-    mode = 0;
+    int m = 2, e = 0;
     if (!(S < 1e300)) {
-      mode = 1; // inf or NaN strengths: keep IEEE propagation (scale 1)
+      m = 1; // inf or NaN strengths: IEEE propagation (scale 1)
     } else if (S > 0.0) {
+      m = 0;
       e = 62 - (int)ceil(log2(1.01 * S));
-      // 2^e must be a normal float, as must the staged scaled strengths;
-      // otherwise double atomics on strengths scaled to at most 1 in magnitude
-      // (staged as float pairs without overflow or underflow)
-      if (e > 120 || e < -126) {
-        mode = 1;
+      if (e > 1000) { // S below about 2^-938: doubles, strengths scaled to at most 1
+        m = 1;
         e = -(int)ceil(log2(S));
       }
     }
+    mode = m;
     scale_d = ldexp(1.0, e);
-    inv_scale = ldexp(1.0, -e);
-    scale_e = e;
+    // the two products divide by 2^64 against weights scaled by 2^62
+    inv_scale = ldexp(1.0, m == 0 ? 4 - e : -e);
   }
   __syncthreads();
+  if (mode == 2) return; // nothing to add (mulfix's offset would not be zero)
   const bool fx = mode == 0;
   const double sc = scale_d;
-  const int lx = lane & 7, lp = lane >> 3;
-  for (int base = warp * 32; base < np; base += nwarp * 32) {
-    const int i = base + lane;
-    if (i < np) {
-      const int p = p0 + i;
-      const int j = L.perm[p];
-      double2 v = ct[j];
-      if (pre) v = cmul_opt<double>(v, pre[j], conj_pre);
-      double kk[NS];
-      const int sx = point_weights<double, NS>(L.loc[0][p], L.bin[0], K, kk);
+  // Work split: thread t owns support row r = t % NPAIR (y = r % NS, z =
+  // r / NS) for group g = t / NPAIR. The subproblem's points are cut into NG
+  // contiguous ranges, one per group, staged SBG per group and batch. A
+  // thread sums its row's NS cells over consecutive points that share their
+  // start cells in registers and adds the sums to the tile when the start
+  // cells change (points are sorted by bin and cell, and clustered points
+  // often share cells), instead of one 64-bit shared add per cell and point.
+  constexpr int NG = 512 / NPAIR; // groups of the 512-thread block
+  constexpr int SBG = SB / NG;    // points per group and batch
+  constexpr int NSLOT = NG * SBG;
+  static_assert(NG >= 1 && SBG >= 1, "staging holds a point per group");
+  const int chunk = (np + NG - 1) / NG;
+  const int nbatch = (chunk + SBG - 1) / SBG;
+  // stage batch bt into buffer k: item t < 3 NSLOT computes dimension
+  // t / NSLOT of slot t % NSLOT (the z weights also give U_z). The items go
+  // to a multiple of four warps (IPW lanes each), so that the FP64 work is
+  // spread over the SM's four schedulers and their FP64 units
+  constexpr int NSTW = 4 * ((3 * NSLOT + 127) / 128), IPW = (3 * NSLOT + NSTW - 1) / NSTW;
+  static_assert(NSTW <= 16 && IPW <= 32, "staging items exceed the block");
+  auto stage = [&](int bt, int k) {
+    unsigned char *stg = stg0 + (size_t)k * SB * PS;
+    const int t = warp * IPW + lane;
+    if (warp < NSTW && lane < IPW && t < 3 * NSLOT) {
+      const int sl = t % NSLOT, d = t / NSLOT;
+      const int g = sl / SBG, i = g * chunk + bt * SBG + (sl - g * SBG);
+      if (i < min(np, (g + 1) * chunk)) {
+        const int p = p0 + i;
+        double kk[NS];
+        // (selects, not a runtime index into the layout, which would copy it
+        // to local memory)
+        const double *ld = d == 0 ? L.loc[0] : (d == 1 ? L.loc[1] : L.loc[2]);
+        const int bd = d == 0 ? L.bin[0] : (d == 1 ? L.bin[1] : L.bin[2]);
+        const int s = point_weights<double, NS>(ld[p], bd, K, kk);
+        unsigned char *P = stg + (size_t)sl * PS;
+        if (d == 2) {
+          const int j = L.perm[p];
+          double2 v = ct[j];
+          if (pre) v = cmul_opt<double>(v, pre[j], conj_pre);
+          const double vr = v.x * sc, vi = v.y * sc;
+          longlong2 *U = reinterpret_cast<longlong2 *>(P);
 #pragma unroll
-      for (int a = 0; a < NS; ++a) {
-        const dfloat d = df_from(kk[a]);
-        kxh[a * SK + lane] = d.h;
-        kxl[a * SK + lane] = d.l;
-      }
-      const int sy = point_weights<double, NS>(L.loc[1][p], L.bin[1], K, kk);
+          for (int a = 0; a < NS; ++a) {
+            if (fx)
+              U[a] = make_longlong2(__double2ll_rn(vr * kk[a]), __double2ll_rn(vi * kk[a]));
+            else
+              U[a] = make_longlong2(__double_as_longlong(vr * kk[a]),
+                                    __double_as_longlong(vi * kk[a]));
+          }
+        } else {
+          int2 *W = reinterpret_cast<int2 *>(P + 16 * NS + 8 * NS * d); // x: 16 NS, y: 24 NS
 #pragma unroll
-      for (int a = 0; a < NS; ++a) {
-        const dfloat d = df_from(kk[a]);
-        kyh[a * SK + lane] = d.h;
-        kyl[a * SK + lane] = d.l;
-      }
-      const int sz = point_weights<double, NS>(L.loc[2][p], L.bin[2], K, kk);
-#pragma unroll
-      for (int a = 0; a < NS; ++a) {
-        const dfloat d = df_from(kk[a]);
-        kzh[a * SK + lane] = d.h;
-        kzl[a * SK + lane] = d.l;
-      }
-      const dfloat vr = df_from(v.x * sc), vi = df_from(v.y * sc);
-      vrh[lane] = vr.h;
-      vrl[lane] = vr.l;
-      vih[lane] = vi.h;
-      vil[lane] = vi.l;
-      spk[lane] = sx | (sy << 10) | (sz << 20);
-    }
-    __syncwarp();
-    const int cnt = min(32, np - base);
-    for (int q = 0; q < cnt; ++q) {
-      const int sp = spk[q];
-      const int rowbase = (sp >> 20) * Q + ((sp >> 10) & 1023) * px + (sp & 1023);
-      const dfloat vr = {vrh[q], vrl[q]}, vi = {vih[q], vil[q]};
-      dfloat ar[NXB], ai[NXB];
-#pragma unroll
-      for (int xb = 0; xb < NXB; ++xb) {
-        const int dx = min(xb * 8 + lx, NS - 1);
-        const dfloat wx = {kxh[dx * SK + q], kxl[dx * SK + q]};
-        ar[xb] = df_mul(vr, wx);
-        ai[xb] = df_mul(vi, wx);
-      }
-#pragma unroll 4
-      for (int r = 0; r < NROUND; ++r) {
-        const int pp = 4 * r + lp;
-        if (pp < NPAIR) {
-          const int dy = pp % NS, dz = pp / NS;
-          const dfloat wyz = df_mul({kyh[dy * SK + q], kyl[dy * SK + q]},
-                                    {kzh[dz * SK + q], kzl[dz * SK + q]});
-          const int a0 = rowbase + dz * Q + dy * px + lx;
-#pragma unroll
-          for (int xb = 0; xb < NXB; ++xb) {
-            if (xb * 8 + lx < NS) {
-              const dfloat tr_ = df_mul(ar[xb], wyz), ti = df_mul(ai[xb], wyz);
-              const int a = a0 + xb * 8;
-              if (fx) {
-                atomicAdd(reinterpret_cast<unsigned long long *>(ire + a),
-                          (unsigned long long)df_to_ll(tr_));
-                atomicAdd(reinterpret_cast<unsigned long long *>(iim + a),
-                          (unsigned long long)df_to_ll(ti));
-              } else {
-                atomicAdd(dre + a, (double)tr_.h + (double)tr_.l);
-                atomicAdd(dim_ + a, (double)ti.h + (double)ti.l);
-              }
+          for (int a = 0; a < NS; ++a) {
+            if (fx) {
+              W[a] = wfix(kk[a]);
+            } else {
+              const long long bits = __double_as_longlong(kk[a]);
+              W[a] = make_int2((int)(bits >> 32), (int)bits);
             }
+          }
+        }
+        // start cell of dimension d (one word each: no read-modify-write
+        // between the three threads of a point)
+        reinterpret_cast<int *>(P + 32 * NS)[d] = s;
+      }
+    }
+  };
+  const int r = threadIdx.x % NPAIR, grp = threadIdx.x / NPAIR;
+  const int dy = r % NS, dz = r / NS;
+  const int gbeg = grp * chunk, gend = min(np, gbeg + chunk);
+  long long accr[NS], acci[NS]; // the run's row sums (mode 1: double bits)
+  int cur = -1;                 // the run's start cells, x | y << 10 | z << 20
+  auto flush = [&]() {
+    const int row = ((cur >> 20) + dz) * Q + (((cur >> 10) & 1023) + dy) * px + (cur & 1023);
+#pragma unroll
+    for (int a = 0; a < NS; ++a) {
+      if (fx) {
+        atomicAdd(reinterpret_cast<unsigned long long *>(ire + row + a),
+                  (unsigned long long)accr[a]);
+        atomicAdd(reinterpret_cast<unsigned long long *>(iim + row + a),
+                  (unsigned long long)acci[a]);
+      } else {
+        atomicAdd(dre + row + a, __longlong_as_double(accr[a]));
+        atomicAdd(dim_ + row + a, __longlong_as_double(acci[a]));
+      }
+    }
+  };
+  stage(0, 0);
+  __syncthreads();
+  int k = 0;
+  for (int bt = 0; bt < nbatch; ++bt, k ^= 1) {
+    if (bt + 1 < nbatch) stage(bt + 1, k ^ 1);
+    const unsigned char *stg = stg0 + (size_t)k * SB * PS;
+    if (grp < NG) {
+      const int cnt = min(SBG, gend - (gbeg + bt * SBG)); // may be <= 0
+      for (int i = 0; i < cnt; ++i) {
+        const unsigned char *P = stg + (size_t)(grp * SBG + i) * PS;
+        const int4 s4 = *reinterpret_cast<const int4 *>(P + 32 * NS);
+        const int sp = s4.x | (s4.y << 10) | (s4.z << 20);
+        if (sp != cur) {
+          if (cur >= 0) flush();
+#pragma unroll
+          for (int a = 0; a < NS; ++a) accr[a] = acci[a] = 0;
+          cur = sp;
+        }
+        const longlong2 U = reinterpret_cast<const longlong2 *>(P)[dz];
+        const int2 wy = reinterpret_cast<const int2 *>(P + 24 * NS)[dy];
+        const int2 *wx = reinterpret_cast<const int2 *>(P + 16 * NS);
+        if (fx) {
+          const long long ur = mulfix(U.x, wy.x, (unsigned)wy.y);
+          const long long ui = mulfix(U.y, wy.x, (unsigned)wy.y);
+#pragma unroll
+          for (int a = 0; a < NS; ++a) {
+            const int2 w = wx[a];
+            accr[a] += mulfix(ur, w.x, (unsigned)w.y);
+            acci[a] += mulfix(ui, w.x, (unsigned)w.y);
+          }
+        } else {
+          const double fy = __longlong_as_double(((long long)wy.x << 32) | (unsigned)wy.y);
+          const double ur = __longlong_as_double(U.x) * fy, ui = __longlong_as_double(U.y) * fy;
+#pragma unroll
+          for (int a = 0; a < NS; ++a) {
+            const int2 w = wx[a];
+            const double f = __longlong_as_double(((long long)w.x << 32) | (unsigned)w.y);
+            accr[a] = __double_as_longlong(__longlong_as_double(accr[a]) + ur * f);
+            acci[a] = __double_as_longlong(__longlong_as_double(acci[a]) + ui * f);
           }
         }
       }
     }
-    __syncwarp();
+    __syncthreads();
   }
+  if (grp < NG && cur >= 0) flush();
   __syncthreads();
   double2 *fwt = fw + (int64_t)tr * nf_total + goff;
   const double is = inv_scale;
-  const int se = scale_e;
   for (int q = threadIdx.x; q < G.cells; q += blockDim.x) {
     const int x = q % G.t[0];
     const int y = (q / G.t[0]) % G.t[1];
@@ -670,11 +685,12 @@ __global__ void __launch_bounds__(256)
     if (fx) {
       const long long a = ire[sidx], bb = iim[sidx];
       if ((a | bb) == 0) continue;
-      v.x = ll_scaled(a, se);
-      v.y = ll_scaled(bb, se);
+      v.x = (double)a * is;
+      v.y = (double)bb * is;
     } else {
       v.x = dre[sidx] * is;
       v.y = dim_[sidx] * is;
+      if (v.x == 0.0 && v.y == 0.0) continue;
     }
     const int64_t g = wrap_idx(G.org[0] + x, L.nf[0]) +
                       (int64_t)L.nf[0] * (wrap_idx(G.org[1] + y, L.nf[1]) +

@@ -77,11 +77,16 @@ __host__ __device__ constexpr size_t tile3v_bytes(int ns, int bx, int by, int bz
           15) / 16 * 16;
 }
 
-// Double-precision 3D spread into an int64 fixed-point tile (variant 4):
-// per-warp staging of 32 points as float pairs (hi, lo) -- x, y and z weights,
-// the two strength components -- and packed start cells.
-__host__ __device__ constexpr int t3x_stage_bytes(int ns) {
-  return (STAGE_STRIDE * (6 * ns + 4) * 4 + STAGE_STRIDE * 4 + 15) / 16 * 16;
+// Double-precision 3D spread into an int64 fixed-point tile (variant 4). The
+// tile is (bin + ns) cells per dimension, unpadded, re and im as int64 planes.
+// Staging: sb points per buffer, two buffers; a point holds U_z (ns x two
+// int64), the y and x weights (ns x two int32 each) and its three start cells.
+__host__ __device__ constexpr int t3x_sb(int ns) { return ns <= 8 ? 128 : (ns <= 11 ? 64 : 32); }
+__host__ __device__ constexpr int t3x_point_bytes(int ns) { return 32 * ns + 16; }
+__host__ __device__ constexpr size_t t3x_tile_bytes(int ncell) { return (size_t)16 * ncell; }
+__host__ __device__ constexpr size_t t3x_bytes(int ns, int bx, int by, int bz) {
+  return t3x_tile_bytes((bx + ns) * (by + ns) * (bz + ns)) +
+         (size_t)2 * t3x_sb(ns) * t3x_point_bytes(ns);
 }
 
 } // namespace gbn

@@ -423,13 +423,14 @@ def test_spread_variants_2d(oracle, dtype, tol):
 
 
 @pytest.mark.parametrize("tol", [1e-7, 1e-9, 1e-12, 1e-14])
-@pytest.mark.parametrize("scale", [1.0, 1e20, 1e200, 1e-200])
+@pytest.mark.parametrize("scale", [1.0, 1e20, 1e200, 1e-200, 1e-290])
 def test_fp64_fixed_point_tile(oracle, tol, scale):
-    """double-precision 3D spread with the int64 fixed-point tile (variant 4,
-    the default for widths above 5) against the double-atomic tile (variant 0)
-    and the FP64 direct sum, on clustered points at strength scales where the
-    tile's power-of-two scale is used (1, 1e20) and where a subproblem falls
-    back to double atomics (1e200, 1e-200)"""
+    """double-precision 3D spread with the int64 fixed-point tile and integer
+    products (variant 4, the default for widths above 5) against the
+    double-atomic tile (variant 0) and the FP64 direct sum, on clustered points
+    at strength scales the tile's power-of-two scale covers (1 to 1e-200) and
+    one where a subproblem's sum needs a scale beyond 2^1000 and falls back to
+    double atomics (1e-290)"""
     import finufft_gb300 as fg
 
     rng = np.random.default_rng(104)
