@@ -142,6 +142,35 @@ __device__ __forceinline__ void eval_kernel(T *ker, T t, const KernelShape<T> &K
   }
 }
 
+// As eval_kernel, using the kernel's evenness for Horner pieces: piece
+// NS-1-j at u is piece j at -u (phi(x) = phi(-x) maps the two intervals onto
+// each other), so with p_j(u) = E_j(u^2) + u O_j(u^2) one pass over piece j's
+// coefficients gives ker[j] = E + u O and ker[NS-1-j] = E - u O: about half
+// the fused multiply-adds of evaluating every piece. The mirrored weights
+// carry piece j's fit error instead of their own piece's (both within the
+// fit target).
+template <typename T, int NS>
+__device__ __forceinline__ void eval_kernel_sym(T *ker, T t, const KernelShape<T> &K) {
+  if (!K.use_horner) {
+    eval_kernel<T, NS>(ker, t, K);
+    return;
+  }
+  constexpr int H = horner_len(NS);
+  const T u = T(2) * t + T(NS - 1);
+  const T w = u * u;
+#pragma unroll
+  for (int j = 0; j < (NS + 1) / 2; ++j) {
+    T e = T(0), o = T(0);
+#pragma unroll
+    for (int k = 0; k < H; ++k) { // coefficient k multiplies u^(H-1-k)
+      if ((H - 1 - k) % 2 == 0) e = fma(e, w, K.coef[k][j]);
+      else o = fma(o, w, K.coef[k][j]);
+    }
+    ker[j] = fma(u, o, e);
+    if (j != NS - 1 - j) ker[NS - 1 - j] = fma(-u, o, e);
+  }
+}
+
 __device__ __forceinline__ void atomic_add_cplx_global(float2 *p, float2 v) {
   atomicAdd(p, v); // vector f32x2 reduction (sm_90 and newer)
 }

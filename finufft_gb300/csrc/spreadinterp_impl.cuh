@@ -461,6 +461,33 @@ __device__ __forceinline__ long long mulfix(long long u, int wh, unsigned wl) {
   const unsigned t3 = __umulhi(ul, (unsigned)wh);
   return t1 + (long long)t2 + (long long)t3 + 1;
 }
+// acc += u W / 2^64 - 1 (mulfix without its centring constant, which a run
+// adds once per point at its flush), with u given as its words (uh, ul) and
+// neg = uh >> 31; one wide and two high multiplies and a carry chain
+__device__ __forceinline__ void mulfix_acc(long long &acc, int uh, unsigned ul, unsigned neg,
+                                           int wh, unsigned wl) {
+  asm("{\n\t"
+      ".reg .u32 t2, t3, m, s2, alo, ahi, plo, phi;\n\t"
+      ".reg .s64 t1;\n\t"
+      "mul.wide.s32 t1, %1, %4;\n\t"
+      "mul.hi.u32 t2, %1, %5;\n\t"
+      "and.b32 m, %5, %3;\n\t"
+      "sub.u32 t2, t2, m;\n\t"
+      "mul.hi.u32 t3, %2, %4;\n\t"
+      "shr.s32 s2, t2, 31;\n\t"
+      "mov.b64 {alo, ahi}, %0;\n\t"
+      "mov.b64 {plo, phi}, t1;\n\t"
+      "add.cc.u32 alo, alo, plo;\n\t"
+      "addc.u32 ahi, ahi, phi;\n\t"
+      "add.cc.u32 alo, alo, t2;\n\t"
+      "addc.u32 ahi, ahi, s2;\n\t"
+      "add.cc.u32 alo, alo, t3;\n\t"
+      "addc.u32 ahi, ahi, 0;\n\t"
+      "mov.b64 %0, {alo, ahi};\n\t"
+      "}"
+      : "+l"(acc)
+      : "r"(uh), "r"(ul), "r"(neg), "r"(wh), "r"(wl));
+}
 // a weight as the (wh, wl) words of round(w 2^62); fitted kernel values can
 // dip a few ulps below zero at the support's edge, and are clamped to 0
 __device__ __forceinline__ int2 wfix(double w) {
@@ -573,7 +600,10 @@ __global__ void __launch_bounds__(512, 1)
         // to local memory)
         const double *ld = d == 0 ? L.loc[0] : (d == 1 ? L.loc[1] : L.loc[2]);
         const int bd = d == 0 ? L.bin[0] : (d == 1 ? L.bin[1] : L.bin[2]);
-        const int s = point_weights<double, NS>(ld[p], bd, K, kk);
+        const double l = ld[p];
+        const double sd = ceil(l - double(NS) * 0.5);
+        const int s = min(max((int)sd + NS / 2, 0), bd); // as point_weights
+        eval_kernel_sym<double, NS>(kk, sd - l, K);
         unsigned char *P = stg + (size_t)sl * PS;
         if (d == 2) {
           const int j = L.perm[p];
@@ -612,15 +642,16 @@ __global__ void __launch_bounds__(512, 1)
   const int gbeg = grp * chunk, gend = min(np, gbeg + chunk);
   long long accr[NS], acci[NS]; // the run's row sums (mode 1: double bits)
   int cur = -1;                 // the run's start cells, x | y << 10 | z << 20
+  int nrun = 0;                 // points in the run (mulfix_acc's offsets)
   auto flush = [&]() {
     const int row = ((cur >> 20) + dz) * Q + (((cur >> 10) & 1023) + dy) * px + (cur & 1023);
 #pragma unroll
     for (int a = 0; a < NS; ++a) {
       if (fx) {
         atomicAdd(reinterpret_cast<unsigned long long *>(ire + row + a),
-                  (unsigned long long)accr[a]);
+                  (unsigned long long)(accr[a] + nrun));
         atomicAdd(reinterpret_cast<unsigned long long *>(iim + row + a),
-                  (unsigned long long)acci[a]);
+                  (unsigned long long)(acci[a] + nrun));
       } else {
         atomicAdd(dre + row + a, __longlong_as_double(accr[a]));
         atomicAdd(dim_ + row + a, __longlong_as_double(acci[a]));
@@ -644,18 +675,23 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll
           for (int a = 0; a < NS; ++a) accr[a] = acci[a] = 0;
           cur = sp;
+          nrun = 0;
         }
+        ++nrun;
         const longlong2 U = reinterpret_cast<const longlong2 *>(P)[dz];
         const int2 wy = reinterpret_cast<const int2 *>(P + 24 * NS)[dy];
         const int2 *wx = reinterpret_cast<const int2 *>(P + 16 * NS);
         if (fx) {
           const long long ur = mulfix(U.x, wy.x, (unsigned)wy.y);
           const long long ui = mulfix(U.y, wy.x, (unsigned)wy.y);
+          const int urh = (int)(ur >> 32), uih = (int)(ui >> 32);
+          const unsigned url = (unsigned)ur, uil = (unsigned)ui;
+          const unsigned urn = (unsigned)(urh >> 31), uin = (unsigned)(uih >> 31);
 #pragma unroll
           for (int a = 0; a < NS; ++a) {
             const int2 w = wx[a];
-            accr[a] += mulfix(ur, w.x, (unsigned)w.y);
-            acci[a] += mulfix(ui, w.x, (unsigned)w.y);
+            mulfix_acc(accr[a], urh, url, urn, w.x, (unsigned)w.y);
+            mulfix_acc(acci[a], uih, uil, uin, w.x, (unsigned)w.y);
           }
         } else {
           const double fy = __longlong_as_double(((long long)wy.x << 32) | (unsigned)wy.y);
