@@ -233,6 +233,29 @@ def take_grid(f, axes_idx):
     return f
 
 
+def cpu_model():
+    """the host CPU's model name and logical core count (lscpu; /proc/cpuinfo
+    when lscpu is missing)"""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if name is None:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith("model name"):
+                    name = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return {"model": name, "logical_cores": os.cpu_count()}
+
+
 def rel_l2(a, b):
     import torch
 
@@ -455,7 +478,7 @@ def run_gpu(args):
                               "deconvolution) of the %d strength vectors over all %d points, "
                               "timed in full (%.2f s; setpts sort %.2f s outside)"
                               % (nt, M, ce, cs),
-                    "execute_s": ce, "setpts_s": cs}
+                    "execute_s": ce, "setpts_s": cs, "host": cpu_model()}
     value = job_value(M * nt, world, ms_batched)
     out = {
         "metric": METRIC, "value": value, "unit": "NU pts/s", "n_gpus": world,
@@ -972,7 +995,7 @@ def run_reference(args):
                                       "deconvolution) of each of the %d strength vectors over "
                                       "all %d points; setpts sort %.2f s outside the steps"
                                       % (nt, M, setpts_s),
-                            "value": v, "unit": "NU pts/s"},
+                            "value": v, "unit": "NU pts/s", "host": cpu_model()},
            "step_s": {"min": min(times), "max": max(times), "median": float(np.median(times))},
            "e2e": {"value": v, "unit": "NU pts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))

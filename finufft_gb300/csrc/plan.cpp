@@ -850,12 +850,31 @@ void Plan<T>::run_type1(const cplx<T> *c, cplx<T> *fk, int ntr, int sign, const 
     GBN_CUDA(cudaMemsetAsync(grid, 0, (size_t)blk * nf_total * sizeof(cplx<T>), stream));
     launch_spread<T>(L, K, cb, pre, conj_pre, grid, nf_total, blk, scfg, stream);
     if (time_stages) GBN_CUDA(cudaEventRecord(ev[1], stream));
-    if (opts.gpu_spreadinterponly) continue;
-    fft(fw.p, sign, true);
-    if (time_stages) GBN_CUDA(cudaEventRecord(ev[2], stream));
-    launch_deconv<T>(dim, ms, nf, opts.modeord, inv, fw.p, nf_total, fkb, blk, stream);
-    if (time_stages) GBN_CUDA(cudaEventRecord(ev[3], stream));
+    if (!opts.gpu_spreadinterponly) {
+      fft(fw.p, sign, true);
+      if (time_stages) GBN_CUDA(cudaEventRecord(ev[2], stream));
+      launch_deconv<T>(dim, ms, nf, opts.modeord, inv, fw.p, nf_total, fkb, blk, stream);
+    } else if (time_stages) {
+      GBN_CUDA(cudaEventRecord(ev[2], stream));
+    }
+    if (time_stages) {
+      GBN_CUDA(cudaEventRecord(ev[3], stream));
+      stage_tick();
+    }
   }
+}
+
+// Stage timing (a diagnostic mode, outside graph capture): waits for the
+// batch's last event and adds its stage intervals to the execute's sums, so
+// that plans running their transforms in several batches report every batch.
+template <typename T> void Plan<T>::stage_tick() {
+  GBN_CUDA(cudaEventSynchronize(ev[3]));
+  float t[4] = {0, 0, 0, 0};
+  cudaEventElapsedTime(&t[0], ev[0], ev[1]);
+  cudaEventElapsedTime(&t[1], ev[1], ev[2]);
+  cudaEventElapsedTime(&t[2], ev[2], ev[3]);
+  cudaEventElapsedTime(&t[3], ev[0], ev[3]);
+  for (int k = 0; k < 4; ++k) stage_acc[k] += t[k];
 }
 
 // Type-2 pipeline on ntr transforms: amplify -> FFT(sign) -> interpolate.
@@ -880,7 +899,10 @@ void Plan<T>::run_type2(const cplx<T> *fk, cplx<T> *c, int ntr, int sign,
       GBN_CUDA(cudaEventRecord(ev[1], stream));
     if (time_stages) GBN_CUDA(cudaEventRecord(ev[2], stream));
     launch_interp<T>(L, K, grid, nf_total, post, conj_post, cb, blk, stream);
-    if (time_stages) GBN_CUDA(cudaEventRecord(ev[3], stream));
+    if (time_stages) {
+      GBN_CUDA(cudaEventRecord(ev[3], stream));
+      stage_tick();
+    }
   }
 }
 
@@ -910,9 +932,11 @@ void Plan<T>::execute_range(cplx<T> *c, cplx<T> *fk, int t0, int nt, bool adjoin
   const bool timed = time_stages && !adjoint;
   const bool tmp_ts = time_stages;
   time_stages = timed;
-  if (timed)
+  if (timed) {
     for (auto &e : ev)
       if (!e) GBN_CUDA(cudaEventCreate(&e));
+    for (float &a : stage_acc) a = 0.f;
+  }
   if (!adjoint) {
     if (type == 1) run_type1(c, fk, nt, iflag, nullptr, 0);
     else if (type == 2) run_type2(fk, c, nt, iflag, nullptr, 0);
@@ -941,19 +965,19 @@ void Plan<T>::execute_range(cplx<T> *c, cplx<T> *fk, int t0, int nt, bool adjoin
                          stream);
       }
     }
-    if (timed) // stage timing of type 3: total only
+    if (timed) { // stage timing of type 3: total only
       for (int k = 3; k >= 1; --k) GBN_CUDA(cudaEventRecord(ev[k], stream));
+      stage_tick();
+    }
   }
   time_stages = tmp_ts;
   GBN_LAUNCH_CHECK();
   if (timed) {
-    // events: ev0 | spread or amplify | ev1 | FFT | ev2 | deconvolve or interp | ev3
-    GBN_CUDA(cudaEventSynchronize(ev[3]));
-    float a = 0, b = 0;
-    cudaEventElapsedTime(&a, ev[0], ev[1]);
-    cudaEventElapsedTime(&times.fft_ms, ev[1], ev[2]);
-    cudaEventElapsedTime(&b, ev[2], ev[3]);
-    cudaEventElapsedTime(&times.total_ms, ev[0], ev[3]);
+    // per batch, events: ev0 | spread or amplify | ev1 | FFT | ev2 | deconvolve
+    // or interp | ev3, summed over the batches by stage_tick
+    const float a = stage_acc[0], b = stage_acc[2];
+    times.fft_ms = stage_acc[1];
+    times.total_ms = stage_acc[3];
     times.spread_or_interp_ms = type == 2 ? b : a;
     times.deconv_ms = type == 2 ? a : b;
     if (type == 3) times.spread_or_interp_ms = times.fft_ms = times.deconv_ms = 0;

@@ -99,6 +99,7 @@ public:
   cudaStream_t stream = nullptr;
   StageTimes times;
   bool time_stages = false;
+  float stage_acc[4] = {0, 0, 0, 0}; // stage sums over an execute's batches
   // sorted point layout (device)
   DevArray<int> perm;
   DevArray<T> loc[3];
@@ -136,6 +137,7 @@ private:
   void make_pruned_fft();
   void make_fseries();
   void sort_points(int64_t M, const T *const xyz[3], const AxisMap ax[3]);
+  void stage_tick();
   void run_type1(const cplx<T> *c, cplx<T> *fk, int ntr, int sign, const cplx<T> *pre,
                  int conj_pre);
   void run_type2(const cplx<T> *fk, cplx<T> *c, int ntr, int sign, const cplx<T> *post,
