@@ -58,7 +58,8 @@ class GbnufftOpts(Structure):
 
     _fields_ = [("planner", c_int), ("spread_variant", c_int), ("fft_prune", c_int),
                 ("spread_float_tile", c_int), ("kernel_form", c_int), ("kerformula", c_int),
-                ("sort_keys", c_int), ("interp_mode", c_int), ("reserved", c_int * 8)]
+                ("sort_keys", c_int), ("interp_mode", c_int), ("batch_cap", c_int),
+                ("reserved", c_int * 7)]
 
 
 class FinufftOpts(Structure):

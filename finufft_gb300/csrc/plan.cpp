@@ -139,16 +139,20 @@ template <typename T> void Plan<T>::make_grid() {
   nf_total = (int64_t)nf[0] * nf[1] * nf[2];
   choose_spread_config(opts.gpu_method != 0);
   if (!opts.gpu_spreadinterponly) {
-    // transforms per batch at most as many as keep their fine grids within half
-    // of L2: a grid that stays in L2 from spread (or amplification) through the
-    // FFT to deconvolution (or interpolation) never travels to HBM (measured on
-    // 16 vectors of 1e7 2D type-2 points, 2048^2 grids: batches of 16 6.6 ms,
-    // of 1 4.8 ms per execute). gpu_maxbatchsize is an upper bound.
+    // 3D type 2: transforms per batch at most as many as keep their fine grids
+    // within half of L2. Each interpolation tile re-reads its halo (3.6x the
+    // bin's cells at 16x12x8 bins and ns 6), cheap while the grid is in L2
+    // (5e6 points, 192^3 grids, 8 vectors: batches of 1 4.70 ms per execute, of
+    // 8 5.29 ms). 2D and type 1 batch freely: the interpolation reuses each
+    // point's weights over the batch's transforms and the batched FFT is more
+    // efficient (2D type 2, 16 vectors of 1e7 points, 2048^2 grids: batches of
+    // 2 6.27 ms, of 16 5.70 ms; 3D type 1 as above: 7.23 against 6.95 ms).
+    // gpu_maxbatchsize is an upper bound; gbnufft_opts.batch_cap = 1 lifts the cap.
     int dev = 0, l2 = 0;
     GBN_CUDA(cudaGetDevice(&dev));
     GBN_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
     const double gbytes = (double)nf_total * sizeof(cplx<T>);
-    if (2.0 * gbytes <= (double)l2)
+    if (ext.batch_cap == 0 && dim == 3 && type == 2 && 2.0 * gbytes <= (double)l2)
       batchsize = std::min(batchsize, std::max(1, (int)((double)l2 / (2.0 * gbytes))));
     destroy_fft();
     fw.resize((size_t)nf_total * batchsize);
@@ -298,7 +302,7 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
       const size_t xsm = spread_tile3x_bytes(ns, bins);
       if (xsm <= (size_t)limit) {
         S.cfg.variant = 4;
-        S.cfg.threads = 512;
+        S.cfg.threads = T3X_THREADS;
         S.cfg.smem = xsm;
         S.smem = xsm;
         return S;

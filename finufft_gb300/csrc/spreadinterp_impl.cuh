@@ -496,7 +496,7 @@ __device__ __forceinline__ int2 wfix(double w) {
 }
 
 template <int NS>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(T3X_THREADS, 1)
     spread_tile3x_kernel(PointLayout<double> L0, KernelShape<double> K,
                          const double2 *__restrict__ c, const double2 *__restrict__ pre,
                          int conj_pre, double2 *__restrict__ fw, int64_t nf_total) {
@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(512, 1)
   // start cells in registers and adds the sums to the tile when the start
   // cells change (points are sorted by bin and cell, and clustered points
   // often share cells), instead of one 64-bit shared add per cell and point.
-  constexpr int NG = 512 / NPAIR; // groups of the 512-thread block
+  constexpr int NG = T3X_THREADS / NPAIR; // groups of the block (launched with T3X_THREADS)
   constexpr int SBG = SB / NG;    // points per group and batch
   constexpr int NSLOT = NG * SBG;
   static_assert(NG >= 1 && SBG >= 1, "staging holds a point per group");
@@ -2053,7 +2053,8 @@ template <typename T, int DIM> struct Dispatch {
           auto kx = spread_tile3x_kernel<NS>;
           GBN_CUDA(cudaFuncSetAttribute(kx, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)cfg.smem));
-          kx<<<grid, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
+          // the kernel's row mapping is built for T3X_THREADS threads
+          kx<<<grid, T3X_THREADS, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
           GBN_LAUNCH_CHECK();
           return;
         }

@@ -81,6 +81,7 @@ __host__ __device__ constexpr size_t tile3v_bytes(int ns, int bx, int by, int bz
 // tile is (bin + ns) cells per dimension, unpadded, re and im as int64 planes.
 // Staging: sb points per buffer, two buffers; a point holds U_z (ns x two
 // int64), the y and x weights (ns x two int32 each) and its three start cells.
+constexpr int T3X_THREADS = 512; // block size the kernel's row mapping assumes
 __host__ __device__ constexpr int t3x_sb(int ns) { return ns <= 8 ? 128 : (ns <= 13 ? 64 : 32); }
 __host__ __device__ constexpr int t3x_point_bytes(int ns) { return 32 * ns + 16; }
 __host__ __device__ constexpr size_t t3x_tile_bytes(int ncell) { return (size_t)16 * ncell; }

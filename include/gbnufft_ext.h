@@ -32,7 +32,10 @@ typedef struct gbnufft_opts {
   int spread_variant; /* -1 auto; tiled spread: 0 shared tile with per-point
                          atomics, 1 one warp per tile (no atomics, same-cell runs in
                          registers), 2 shared tile with same-cell register runs,
-                         3 (3D) as 2 with x-slack runs and vector staging (ns <= 8) */
+                         3 (3D) as 2 with x-slack runs and vector staging (ns <= 8),
+                         4 (3D double precision, the default for ns >= 6) an int64
+                         fixed-point tile with integer products, one thread per
+                         support row summing runs of points in registers */
   int fft_prune;      /* 1: 2D/3D FFTs as a 1D pass along x plus passes over the other
                          dimensions on the x columns of the retained modes only
                          (measured slower than one cuFFT plan on GB300; default 0) */
@@ -59,7 +62,12 @@ typedef struct gbnufft_opts {
                          directly; 3 tiles copied by the tensor memory accelerator
                          (bulk tensor copies, two buffers: the next transform's tile
                          loads while the current one is interpolated) */
-  int reserved[8];
+  int batch_cap;      /* 0 (default): 3D type-2 plans run at most as many transforms
+                         per batch as keep their fine grids within half of L2 (the
+                         interpolation tiles re-read their halos); other plans
+                         batch gpu_maxbatchsize transforms; 1: gpu_maxbatchsize as
+                         given everywhere */
+  int reserved[7];
 } gbnufft_opts;
 
 typedef struct gbnufft_plan_info {

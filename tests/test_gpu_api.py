@@ -439,3 +439,48 @@ def test_trim_scratch_then_setpts(oracle, engine):
     # the sort is deterministic; atomics add in any order (float rounding)
     assert oracle.rel_l2(b, a) < 1e-6
     assert engine.gbnufft_trim_scratch(999) != 0
+
+
+def test_batch_cap_and_stage_times():
+    """3D type-2 plans keep a batch's fine grids within half of L2 unless
+    batch_cap = 1; 2D plans run gpu_maxbatchsize transforms per batch; the
+    stage times of an execute in several batches cover every batch"""
+    import torch
+
+    import finufft_gb300 as fg
+
+    l2 = torch.cuda.get_device_properties(0).L2_cache_size
+    nt = 8
+    nm3 = (64, 64, 64)
+    p3 = fg.Plan(2, nm3, n_trans=nt, eps=1e-5, gpu_maxbatchsize=nt)
+    gbytes = float(np.prod(p3.info().nf)) * 8
+    expect = min(nt, max(1, int(l2 / (2 * gbytes)))) if 2 * gbytes <= l2 else nt
+    assert p3.info().batchsize == expect
+    assert fg.Plan(2, nm3, n_trans=nt, eps=1e-5, gpu_maxbatchsize=nt,
+                   batch_cap=1).info().batchsize == nt
+    assert fg.Plan(2, (512, 512), n_trans=nt, eps=1e-5,
+                   gpu_maxbatchsize=nt).info().batchsize == nt
+    # stage times against the execute's own duration, several batches
+    rng = np.random.default_rng(106)
+    M = 400_000
+    pts = [_dev(rng.uniform(-np.pi, np.pi, M).astype(np.float32)) for _ in range(3)]
+    p = fg.Plan(2, nm3, n_trans=nt, eps=1e-5, gpu_maxbatchsize=3, batch_cap=1)
+    assert p.info().batchsize == 3
+    p.setpts(*pts)
+    fk = torch.randn(nt, *nm3, 2, device="cuda").view(torch.complex64)[..., 0]
+    c = torch.empty(nt, M, dtype=torch.complex64, device="cuda")
+    p.execute(fk, out=c)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    p.execute(fk, out=c)
+    e1.record()
+    torch.cuda.synchronize()
+    whole = e0.elapsed_time(e1)
+    p.stage_times(True)
+    p.execute(fk, out=c)
+    torch.cuda.synchronize()
+    st = p.stage_times(False)
+    # three batches: the last alone would be about a third of the whole
+    assert st[3] > 0.7 * whole, (st, whole)
+    assert abs(st[0] + st[1] + st[2] - st[3]) < 0.05 * st[3] + 0.05, st
