@@ -73,6 +73,8 @@ Plan<T>::Plan(int type_, int dim_, const int64_t *modes_in, int iflag_, int ntra
       tol(tol_), opts(opts_) {
   if (ext_) ext = *ext_;
   else gbnufft_default_opts(&ext);
+  // planners 0 and 1 are fixed rules; 2 and 3 set this at setpts (1 on fallback)
+  planner_used = (ext.planner == 1) ? 1 : 0;
   if (dim < 1 || dim > 3) GBN_THROW(FINUFFT_ERR_DIM_NOTVALID, "dim");
   DeviceScope ds(opts.gpu_device_id);
   if (type < 1 || type > 3) {
@@ -189,10 +191,11 @@ SpreadSetup spread_setup(int dim, int ns, const int nf[3], const cufinufft_opts 
   const int threads = (dim == 3 && !std::is_same_v<T, float>) ? 128 : 256;
   int def = dim == 1 ? 1024 : (dim == 2 ? 32 : 8);
   if (ext.planner == 1) {
-    // the reference library's bin sizes (src/cuda/heuristics.cu:50-57,378-392):
-    // 1D 1024, 2D 40, 3D from a shared-memory budget of 50/90/100% by width
-    def = dim == 1 ? 1024 : (dim == 2 ? 40 : 0);
-    if (dim == 3) {
+    // the reference library's bin sizes (src/cuda/heuristics.cu:50-57,373-392):
+    // method 1 (its default for type 2) 1D 1024, 2D 40, 3D 8; method 2 1D 1024,
+    // 2D 40, 3D from a shared-memory budget of 50/90/100% by width
+    def = dim == 1 ? 1024 : (dim == 2 ? 40 : (opts.gpu_method == 1 ? 8 : 0));
+    if (dim == 3 && def == 0) {
       const double load = ns <= 6 ? 0.5 : (ns <= 10 ? 0.9 : 1.0);
       auto fit = [&](double bytes) {
         const double elems = std::floor(bytes / (2.0 * sizeof(T)));
@@ -357,7 +360,11 @@ template SpreadSetup spread_setup<double>(int, int, const int[3], const cufinuff
                                           const gbnufft_opts &, bool);
 
 template <typename T> void Plan<T>::choose_spread_config(bool user_method) {
-  const SpreadSetup S = spread_setup<T>(dim, K.ns, nf, opts, ext, user_method);
+  // the reference heuristic's automatic method (src/cuda/makeplan.cu:310-314):
+  // method 2 for types 1 and 3, method 1 (per-point interpolation) for type 2
+  cufinufft_opts o = opts;
+  if (ext.planner == 1 && o.gpu_method == 0 && type == 2) o.gpu_method = 1;
+  const SpreadSetup S = spread_setup<T>(dim, K.ns, nf, o, ext, user_method);
   for (int d = 0; d < 3; ++d) {
     bins[d] = S.bins[d];
     nbins[d] = S.nbins[d];
@@ -452,7 +459,9 @@ template <typename T> void Plan<T>::apply_shape(const Candidate &c) {
     o.gpu_maxsubprobsize = c.maxsub;
     e.spread_variant = c.variant;
   }
-  o.gpu_method = 0;
+  // the reference heuristic's slot takes its automatic method too: 1 (per-point
+  // interpolation) for type 2, else 2
+  o.gpu_method = (c.reference && type == 2) ? 1 : 0;
   const SpreadSetup S = spread_setup<T>(dim, K.ns, nf, o, e, false);
   for (int d = 0; d < 3; ++d) {
     bins[d] = S.bins[d];
@@ -615,7 +624,10 @@ template <typename T> PointLayout<T> Plan<T>::layout() const {
   L.perm = perm.p;
   L.cell_sorted = cell_sorted;
   L.sorted_out = isort.p;
-  L.interp_mode = ext.interp_mode;
+  // method 1 (asked for, or the reference heuristic's choice for type 2)
+  // interpolates one point per thread from the grid, as the reference's
+  // method 1 does; method 2 uses the tiled schedules
+  L.interp_mode = (method == 1 && ext.interp_mode == 0) ? 1 : ext.interp_mode;
   return L;
 }
 
@@ -666,16 +678,18 @@ void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]
   sub_start_.p = sa.start;
   sub_count_.p = sa.count;
   sub_bin_.n = sub_start_.n = sub_count_.n = sa.cap;
-  // type 2 batches whose per-transform output fits in L2: interpolate into
-  // sorted order, then scatter transform by transform (measured on 16 vectors
-  // of 1e7 2D points: 6.3 -> 5.8 ms; the interpolation alone runs at 2.4 ms
-  // once the scattered 8-byte writes are out of it). The sorted copy of a
+  // 2D type-2 batches whose per-transform output fits in L2: interpolate into
+  // sorted order, then scatter transform by transform (16 vectors of 1e7 2D
+  // points, batches of 16: 5.72 ms against 6.84 ms writing user order from the
+  // interpolation). Not in 3D, where the interpolation's own scattered writes
+  // cost less than the extra pass (1.25e7 clustered points, 4 vectors at 128^3:
+  // 4.98 ms direct, 5.85 ms through the sorted copy). The sorted copy of a
   // batch's outputs is only taken when it costs at most an eighth of the
   // device memory free at setpts. gbnufft_opts.interp_mode 1 or 2 writes user
   // order directly.
   isort.release();
-  if (type == 2 && batchsize > 1 && batchsize <= 65535 && dim >= 2 && M > 0 &&
-      ext.interp_mode == 0) { // (the scatter's grid has one row per transform)
+  if (type == 2 && batchsize > 1 && batchsize <= 65535 && dim == 2 && M > 0 &&
+      ext.interp_mode == 0 && method != 1) { // (the scatter's grid has one row per transform)
     int dev = 0, l2 = 0;
     GBN_CUDA(cudaGetDevice(&dev));
     GBN_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));

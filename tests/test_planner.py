@@ -246,3 +246,51 @@ def test_candidate_rejection_rule(engine, oracle):
                         if not dbl and sigma < 2 and tol < 1e-5:
                             want = False
                         assert v.value == int(want), (dbl, dim, ty, tol, k)
+
+
+def _reference_bins(dim, ns, dbl, method, limit):
+    """bin sizes of the reference heuristic (src/cuda/heuristics.cu:50-57 and
+    373-392) for a device whose per-block shared-memory opt-in limit is limit"""
+    if method == 1 or dim < 3:
+        b = 1024 if dim == 1 else (40 if dim == 2 else 8)
+        return [b if d < dim else 1 for d in range(3)]
+    csize = 16 if dbl else 8
+
+    def fit(mem):
+        return int(math.floor((mem // csize) ** (1.0 / 3.0))) - (ns + 1)
+
+    load = 0.5 if ns <= 6 else (0.9 if ns <= 10 else 1.0)
+    b = fit(int(limit * load))
+    if b < 1:
+        b = fit(limit)
+    return [b, b, b]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype,tol", [("complex64", 1e-5), ("complex64", 1e-7),
+                                       ("complex128", 1e-9), ("complex128", 1e-12)])
+@pytest.mark.parametrize("ty", [1, 2])
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_reference_heuristic_planner(dtype, tol, ty, dim):
+    """planner 1 restates the reference heuristic: method 2 for type 1 and
+    method 1 for type 2 when the method is automatic (src/cuda/makeplan.cu:
+    310-314), bins from src/cuda/heuristics.cu for that method, 1024-point
+    subproblems and sigma 2 for types 1 and 2"""
+    import torch
+
+    import finufft_gb300 as fg
+
+    limit = torch.cuda.get_device_properties(0).shared_memory_per_block_optin
+    nm = {1: (200,), 2: (40, 48), 3: (24, 20, 16)}[dim]
+    plan = fg.Plan(ty, nm, eps=tol, dtype=dtype, planner=1)
+    info = plan.info()
+    method = 2 if ty == 1 else 1
+    # the reference falls back to method 1 when its method-2 tile does not fit
+    # (src/cuda/makeplan.cu:315-322); this engine's padded tile at the
+    # reference's 3D bins for wide kernels does not, and falls back the same way
+    fallback = ty == 1 and dim == 3 and info.method == 1
+    assert info.method == method or fallback
+    assert list(info.bins) == _reference_bins(dim, info.ns, dtype == "complex128", method, limit)
+    assert info.upsampfac == 2.0
+    assert info.maxsubprobsize == 1024
+    assert info.kernel_form == 1  # ES, as the reference GPU library
