@@ -550,6 +550,10 @@ Candidate Plan<T>::plan_shape(int64_t Mp, const T *const xyz[3], int64_t Np) {
           best = k;
         }
       }
+      Candidate c0;
+      if (best > 0 && planner_candidate(dim, dbl, 0, &c0) && candidate_valid(c0) &&
+          pred[0] <= best_ms * PLANNER_KEEP_DEFAULT)
+        best = 0;
     }
   } else if (type != 3 && Mp > 0) {
     // autotuner: time every valid candidate on a strided sample of the points,
@@ -645,6 +649,11 @@ void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]
   uint64_t sbinvol = 1;
   for (int d = 0; d < dim; ++d) sbinvol *= (uint64_t)bins[d] + 1;
   int cell_keys = (uint64_t)nb * binvol0 <= 0xffffffffull ? 1 : 0;
+  // gbnufft_opts.sort_keys = 2: bin keys only, the reference's ordering (bin
+  // index x fastest, include/cufinufft/spreadinterp.hpp:139-150; points of a
+  // bin in input order, as the CPU library's stable counting sort,
+  // include/finufft/spread.hpp:459-584)
+  if (ext.sort_keys == 2) cell_keys = 0;
   // gbnufft_opts.sort_keys = 1 keeps whole-cell keys for odd widths too
   if (cell_keys && K.ns % 2 == 1 && (uint64_t)nb * sbinvol <= 0xffffffffull &&
       ext.sort_keys != 1)

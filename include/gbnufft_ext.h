@@ -54,7 +54,9 @@ typedef struct gbnufft_opts {
   int kerformula;     /* PSWF shape parameter choice as finufft_opts.spread_kerformula:
                          0 or 8 (default), 7, 9; other values are rejected */
   int sort_keys;      /* 0 (default): points sorted by bin and, inside the bin, by the
-                         first cell of their kernel support; 1: by bin and cell */
+                         first cell of their kernel support; 1: by bin and cell;
+                         2: by bin only, points of a bin in input order (the
+                         reference's bin ordering; fewer same-cell runs) */
   int interp_mode;    /* type 2 interpolation: 0 auto (3 where its boxes fit, else 2, and
                          batches may write sorted order and scatter it per transform);
                          1 one thread per point gathering from the grid; 2 tiles loaded

@@ -255,7 +255,7 @@ static void or_axis(double x, double shift, double scale, int nf, int bin, int f
  * sort does for float plans). Returns 0. */
 int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *shift,
                 const double *scale, const int *nf, const int *bin, int32_t *perm,
-                void *loc, int loc_is_float, int float_inputs, int ns) {
+                void *loc, int loc_is_float, int float_inputs, int ns, int bin_only) {
   int nb[3] = {1, 1, 1};
   int bn[3] = {1, 1, 1};
   for (int d = 0; d < dim; ++d) {
@@ -264,7 +264,10 @@ int or_bin_sort(int dim, int64_t M, const double *const *coords, const double *s
   }
   const uint64_t nbins = (uint64_t)nb[0] * nb[1] * nb[2];
   uint64_t binvol = (uint64_t)bn[0] * bn[1] * bn[2];
-  const int cell_keys = nbins * binvol <= 0xffffffffull;
+  /* bin_only: the reference's ordering, bin index (x fastest) and input order
+   * within a bin (include/cufinufft/spreadinterp.hpp:139-150,
+   * include/finufft/spread.hpp:459-584) */
+  const int cell_keys = !bin_only && nbins * binvol <= 0xffffffffull;
   /* odd kernel widths: start-cell keys (cell + 1 when the fraction is at
    * least one half, so bin + 1 values per dimension) when they still fit 32
    * bits, as the engine's sort */

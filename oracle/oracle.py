@@ -49,7 +49,7 @@ def lib():
         L.or_fine_grid.argtypes = [I64, d, i]
         L.or_fine_grid.restype = I64
         L.or_type3_grid.argtypes = [d, d, d, i, P]
-        L.or_bin_sort.argtypes = [i, I64, P, P, P, P, P, P, P, i, i, i]
+        L.or_bin_sort.argtypes = [i, I64, P, P, P, P, P, P, P, i, i, i, i]
         L.or_fold_many.argtypes = [I64, P, i, i, P, P]
         L.or_dirft1.argtypes = [i, I64, P, P, i, P, I64, P, P]
         L.or_dirft2.argtypes = [i, I64, P, i, P, P, I64, P, P]
@@ -268,11 +268,13 @@ def fold_positions(x, nf, f32):
     return cell[:len(x)], frac[:len(x)]
 
 
-def bin_sort(xs, nf, bins, shift=None, scale=None, loc_dtype=np.float32, ns=0):
+def bin_sort(xs, nf, bins, shift=None, scale=None, loc_dtype=np.float32, ns=0, bin_only=False):
     """Host replica of the device bin sort: (perm, loc[dim, M]); ns = the plan's
     kernel width (odd widths sort by the start cell of the support, the cell
     or the next one when the fraction is at least one half, when the keys fit
-    32 bits)."""
+    32 bits); bin_only: the reference's ordering, bin index with x fastest and
+    input order within a bin (include/cufinufft/spreadinterp.hpp:139-150,
+    include/finufft/spread.hpp:459-584)."""
     dim = len(xs)
     float_inputs = all(np.asarray(x).dtype == np.float32 for x in xs)
     xs = _coords(xs)
@@ -285,7 +287,7 @@ def bin_sort(xs, nf, bins, shift=None, scale=None, loc_dtype=np.float32, ns=0):
     loc = np.zeros((dim, max(M, 1)), dtype=loc_dtype)
     lib().or_bin_sort(dim, M, _ptrs(xs), _ptr(shift), _ptr(scale), _ptr(nfa), _ptr(ba),
                       _ptr(perm), _ptr(loc), int(loc_dtype == np.float32), int(float_inputs),
-                      int(ns))
+                      int(ns), int(bin_only))
     return perm[:M], loc[:, :M]
 
 

@@ -146,9 +146,12 @@ def test_type3(oracle, dtype, dim, form):
 
 @pytest.mark.parametrize("dtype", ["complex64", "complex128"])
 @pytest.mark.parametrize("dim", [1, 2, 3])
-def test_sort_bit_exact(oracle, dtype, dim):
+@pytest.mark.parametrize("keys", [0, 2])
+def test_sort_bit_exact(oracle, dtype, dim, keys):
     """setpts' device permutation and bin-local coordinates equal the host
-    replica (stable counting sort with the engine's fold) bit for bit."""
+    replica (stable counting sort with the engine's fold) bit for bit, with the
+    engine's keys (bin and support start cell, 0) and with the reference's bin
+    ordering (bin index x fastest, input order inside a bin, 2)."""
     import ctypes
 
     import finufft_gb300 as fg
@@ -165,7 +168,7 @@ def test_sort_bit_exact(oracle, dtype, dim):
     nm = CASES[dim][0]
     # even and odd kernel widths (odd ones sort by half cell)
     for tol in ((1e-5, 1e-6) if rdt == np.float32 else (1e-10, 1e-12)):
-        plan = fg.Plan(1, nm, eps=tol, dtype=dtype)
+        plan = fg.Plan(1, nm, eps=tol, dtype=dtype, sort_keys=keys)
         plan.setpts(*[_dev(p) for p in pts])
         info = plan.info()
         perm = np.zeros(M, dtype=np.int32)
@@ -176,7 +179,7 @@ def test_sort_bit_exact(oracle, dtype, dim):
         # plans, which take the single-precision fold), fastest axis first
         hperm, hloc = oracle.bin_sort([np.ascontiguousarray(p) for p in pts[::-1]],
                                       list(info.nf)[:dim], list(info.bins)[:dim], loc_dtype=rdt,
-                                      ns=info.ns)
+                                      ns=info.ns, bin_only=keys == 2)
         np.testing.assert_array_equal(perm, hperm)
         np.testing.assert_array_equal(loc.reshape(dim, M), hloc)
 
@@ -505,3 +508,33 @@ def test_interp_modes_agree(oracle, dim, dtype, ntr):
     same = oracle.nufft_es(2, _oracle_pts(pts), fk[k], -1, tol, n_modes=nm[::-1],
                            is_float=dtype == "complex64", kernel=_kernel(plan))
     assert oracle.rel_l2(outs[3][k], ref) < _bound(oracle.rel_l2(same, ref), dtype)
+
+
+@pytest.mark.parametrize("dtype,tol", [("complex64", 1e-5), ("complex128", 1e-12)])
+@pytest.mark.parametrize("ty", [1, 2])
+def test_reference_bin_ordering_transforms(oracle, dtype, tol, ty):
+    """3D plans sorted in the reference's bin ordering (sort_keys = 2, no
+    support-cell refinement inside a bin) give the default plan's result to
+    rounding and the FP64 direct sum within the bar"""
+    import finufft_gb300 as fg
+
+    rdt = np.float32 if dtype == "complex64" else np.float64
+    rng = np.random.default_rng(108 + ty)
+    nm, M = (14, 16, 12), 8000
+    pts = _clustered(rng, 3, M, rdt)
+    data = _cx(rng, M if ty == 1 else nm, dtype)
+    outs = []
+    for keys in (0, 2):
+        plan = fg.Plan(ty, nm, eps=tol, dtype=dtype, isign=1 if ty == 1 else -1, sort_keys=keys)
+        plan.setpts(*[_dev(p) for p in pts])
+        outs.append(plan.execute(_dev(data)).cpu().numpy().ravel())
+    assert oracle.rel_l2(outs[1], outs[0]) < (2e-6 if dtype == "complex64" else 1e-13)
+    if ty == 1:
+        ref = oracle.dirft1(_oracle_pts(pts), data, 1, nm[::-1])
+        same = oracle.nufft_es(1, _oracle_pts(pts), data, 1, tol, n_modes=nm[::-1],
+                               is_float=dtype == "complex64", kernel=_kernel(plan))
+    else:
+        ref = oracle.dirft2(_oracle_pts(pts), data.ravel(), -1, nm[::-1])
+        same = oracle.nufft_es(2, _oracle_pts(pts), data, -1, tol, n_modes=nm[::-1],
+                               is_float=dtype == "complex64", kernel=_kernel(plan))
+    assert oracle.rel_l2(outs[1], ref) < _bound(oracle.rel_l2(np.ravel(same), ref), dtype)

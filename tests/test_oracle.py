@@ -224,3 +224,30 @@ def test_single_precision_fold_matches_fp64_fold(oracle):
         same = c1 == c0
         edge = np.minimum(f0, 1 - f0) < 1e-6
         assert (same | edge).all(), nf
+
+
+def test_bin_sort_reference_ordering(oracle):
+    """bin_only: the reference's bin ordering -- bin index floor(folded cell /
+    bin) with x fastest (include/cufinufft/spreadinterp.hpp:139-150) and
+    points of a bin in input order, as the CPU library's stable counting sort
+    (include/finufft/spread.hpp:459-584) -- computed here independently"""
+    rng = np.random.default_rng(5)
+    M = 6000
+    xs = [rng.uniform(-np.pi, np.pi, M) for _ in range(3)]
+    xs[0][:10] = np.pi
+    xs[2][10:20] = -np.pi
+    nf, bins = [40, 30, 20], [8, 7, 6]
+    nb = [(nf[d] + bins[d] - 1) // bins[d] for d in range(3)]
+    for ns in (6, 7):
+        perm, _ = oracle.bin_sort(xs, nf, bins, loc_dtype=np.float64, ns=ns, bin_only=True)
+        b = []
+        for d in range(3):
+            r = np.mod(xs[d] / (2 * np.pi) + 0.5, 1.0) * nf[d]
+            b.append(np.minimum(np.floor(r).astype(np.int64), nf[d] - 1) // bins[d])
+        binid = b[0] + nb[0] * (b[1] + nb[1] * b[2])
+        expect = np.argsort(binid, kind="stable")
+        # away from float ties at bin edges the numpy fold agrees with the exact one
+        assert np.mean(perm == expect) > 0.999, ns
+        ks = binid[perm]
+        same = np.diff(ks) == 0
+        assert np.all(np.diff(perm)[same] > 0), ns
