@@ -487,9 +487,12 @@ double Plan<T>::time_candidate(const Candidate &c, int64_t Ms, const T *const xs
   for (int d = 0; d < 3; ++d) ax[d] = AxisMap{0.0, 1.0, nf[d], bins[d]};
   sort_points(Ms, xs, ax);
   const PointLayout<T> L = layout();
-  AsyncBuf cv((size_t)std::max<int64_t>(Ms, 1) * sizeof(cplx<T>), stream);
-  GBN_CUDA(cudaMemsetAsync(cv.p, 0x3c, (size_t)std::max<int64_t>(Ms, 1) * sizeof(cplx<T>),
-                           stream)); // any finite nonzero strengths
+  // the batch's transforms together, as execute runs them (the FFT plan is the
+  // batch's; batched interpolation reuses each point's weights)
+  const int nt = std::max(1, batchsize);
+  const size_t cbytes = (size_t)std::max<int64_t>(Ms, 1) * nt * sizeof(cplx<T>);
+  AsyncBuf cv(cbytes, stream);
+  GBN_CUDA(cudaMemsetAsync(cv.p, 0x3c, cbytes, stream)); // any finite nonzero strengths
   cudaEvent_t e0, e1, e2;
   GBN_CUDA(cudaEventCreate(&e0));
   GBN_CUDA(cudaEventCreate(&e1));
@@ -498,9 +501,9 @@ double Plan<T>::time_candidate(const Candidate &c, int64_t Ms, const T *const xs
   for (int rep = 0; rep < 3; ++rep) {
     GBN_CUDA(cudaEventRecord(e0, stream));
     if (type == 1)
-      launch_spread<T>(L, K, cv.as<cplx<T>>(), nullptr, 0, fw.p, nf_total, 1, scfg, stream);
+      launch_spread<T>(L, K, cv.as<cplx<T>>(), nullptr, 0, fw.p, nf_total, nt, scfg, stream);
     else
-      launch_interp<T>(L, K, fw.p, nf_total, nullptr, 0, cv.as<cplx<T>>(), 1, stream);
+      launch_interp<T>(L, K, fw.p, nf_total, nullptr, 0, cv.as<cplx<T>>(), nt, stream);
     GBN_CUDA(cudaEventRecord(e1, stream));
     fft(fw.p, 1, type == 1);
     GBN_CUDA(cudaEventRecord(e2, stream));

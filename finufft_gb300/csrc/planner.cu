@@ -393,8 +393,13 @@ bool planner_predict(const float feat[PLANNER_NF], double ms_out[PLANNER_K], cud
   if (!m.trained) return false;
   float z[PLANNER_NF];
   for (int f = 0; f < PLANNER_NF; ++f) {
-    if (feat[f] < m.lo[f] || feat[f] > m.hi[f]) return false; // outside the training range
-    z[f] = m.stdev[f] > 0 ? (feat[f] - m.mean[f]) / m.stdev[f] : 0.0f;
+    float v = feat[f];
+    // log2 of the transforms per batch saturates at the top of the model's
+    // range: more transforms scale every slot's time alike (the sweeps batch
+    // at most 4), so the ranking the model gives there holds
+    if (f == 6 && v > m.hi[f]) v = m.hi[f];
+    if (v < m.lo[f] || v > m.hi[f]) return false; // outside the training range
+    z[f] = m.stdev[f] > 0 ? (v - m.mean[f]) / m.stdev[f] : 0.0f;
   }
   float *w = nullptr;
   GBN_CUDA(cudaGetSymbolAddress((void **)&w, g_planner_w));
