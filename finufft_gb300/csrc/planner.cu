@@ -197,7 +197,7 @@ void point_features(int dim, int type, bool dbl, int64_t M, const T *const xyz[3
   feat[3] = (float)std::log10((double)M + 1.0);
   feat[4] = (float)std::log10(nmodes + 1.0);
   feat[5] = (float)(-std::log10(tol));
-  feat[6] = (float)std::log2((double)std::max(ntr, 1));
+  feat[PLANNER_F_BATCH] = (float)std::log2((double)std::max(ntr, 1));
   feat[7] = (float)(std::sqrt(var) / mean);
   feat[8] = (float)(1.0 - st[2] / cells);
   feat[9] = (float)std::log10(std::max(st[3], 1.0) / mean);
@@ -397,7 +397,7 @@ bool planner_predict(const float feat[PLANNER_NF], double ms_out[PLANNER_K], cud
     // log2 of the transforms per batch saturates at the top of the model's
     // range: more transforms scale every slot's time alike (the sweeps batch
     // at most 4), so the ranking the model gives there holds
-    if (f == 6 && v > m.hi[f]) v = m.hi[f];
+    if (f == PLANNER_F_BATCH && v > m.hi[f]) v = m.hi[f];
     if (v < m.lo[f] || v > m.hi[f]) return false; // outside the training range
     z[f] = m.stdev[f] > 0 ? (v - m.mean[f]) / m.stdev[f] : 0.0f;
   }

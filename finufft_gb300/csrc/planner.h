@@ -16,6 +16,7 @@
 namespace gbn {
 
 constexpr int PLANNER_NF = 12; // input features
+constexpr int PLANNER_F_BATCH = 6; // feature: log2 of the transforms per batch
 constexpr int PLANNER_H = 64;  // width of each of the two hidden layers
 constexpr int PLANNER_K = 12;  // candidate slots (outputs)
 // parameters: W1[H][NF] b1[H] W2[H][H] b2[H] W3[K][H] b3[K]
