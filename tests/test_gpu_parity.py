@@ -528,7 +528,9 @@ def test_reference_bin_ordering_transforms(oracle, dtype, tol, ty):
         plan = fg.Plan(ty, nm, eps=tol, dtype=dtype, isign=1 if ty == 1 else -1, sort_keys=keys)
         plan.setpts(*[_dev(p) for p in pts])
         outs.append(plan.execute(_dev(data)).cpu().numpy().ravel())
-    assert oracle.rel_l2(outs[1], outs[0]) < (2e-6 if dtype == "complex64" else 1e-13)
+    # the orderings flush different register runs into the fixed-point tile,
+    # each rounded to at most 2^-29 of its subproblem's strength sum
+    assert oracle.rel_l2(outs[1], outs[0]) < (5e-6 if dtype == "complex64" else 1e-13)
     if ty == 1:
         ref = oracle.dirft1(_oracle_pts(pts), data, 1, nm[::-1])
         same = oracle.nufft_es(1, _oracle_pts(pts), data, 1, tol, n_modes=nm[::-1],
