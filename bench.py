@@ -741,8 +741,13 @@ def cfg_c4(args, dev, stream, with_cpu=True):
     plan = ctypes.c_void_p()
     o = _lib.default_opts()
     o.gpu_stream = stream.cuda_stream
+    ext = None
+    if args.variant >= 0:  # tuning runs: the 2D spread variant of the batch
+        ext = _lib.default_ext_opts()
+        ext.spread_variant = args.variant
     assert lib.cufinufftf_batch_makeplan(1, 2, nprob, nm.ctypes.data_as(
-        ctypes.POINTER(ctypes.c_int64)), 1, tol, ctypes.byref(plan), ctypes.byref(o), None) == 0
+        ctypes.POINTER(ctypes.c_int64)), 1, tol, ctypes.byref(plan), ctypes.byref(o),
+        ctypes.byref(ext) if ext is not None else None) == 0
     t0 = time.perf_counter()
     assert lib.cufinufftf_batch_setpts(plan, Ms.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
                                        xy[0].data_ptr(), xy[1].data_ptr(), None) == 0
