@@ -229,12 +229,13 @@ def test_spread_variants_3d(oracle, dtype, tol, bins):
 
 
 @pytest.mark.parametrize("tol", [1e-3, 1e-5])
-@pytest.mark.parametrize("scale", [1.0, 1e25, 1e-20])
+@pytest.mark.parametrize("scale", [1.0, 1e25, 1e-20, 1e31])
 def test_fixed_point_tile(oracle, tol, scale):
     """single-precision 3D spread with the int32 fixed-point tile (the default
     for ns <= 6) against the float tile and the FP64 direct sum, on clustered
     points with a few strong sources among weak ones, at strength scales far
-    from 1 (the per-subproblem scale follows them)"""
+    from 1 (the per-subproblem power-of-two scale follows them; at 1e31 the
+    subproblems' strength sums exceed 2^100 and they add floats instead)"""
     import finufft_gb300 as fg
 
     rng = np.random.default_rng(101)
