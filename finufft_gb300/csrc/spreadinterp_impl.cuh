@@ -970,11 +970,17 @@ __device__ __forceinline__ double2 vmake(const double *e) { return make_double2(
 // for a dense 4096-point subproblem, against 24 for a float tile rounded at
 // every add).
 // A subproblem whose S is outside (2^-96, 2^100), inf or NaN keeps float atomics.
+//
+// Grid: the ntr transforms of a batch are interleaved fastest, ntrx of them
+// per subproblem along x (block x = sub * ntrx + t), the remaining groups of
+// ntrx along y. The blocks of one subproblem then run close together and all
+// but the first find the subproblem's sorted coordinates and permutation in
+// L2 rather than streaming them from HBM once per transform.
 template <typename T, int NS, bool FX = false>
 __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
     spread_tile3v_kernel(PointLayout<T> L0, KernelShape<T> K, const cplx<T> *__restrict__ c,
                          const cplx<T> *__restrict__ pre, int conj_pre,
-                         cplx<T> *__restrict__ fw, int64_t nf_total) {
+                         cplx<T> *__restrict__ fw, int64_t nf_total, int ntrx, int ntr) {
   using V = typename Vec16<T>::type;
   constexpr int TS = (int)sizeof(T);
   constexpr int VW = t3v_vw(TS), NR = t3v_nr(NS), NRV = t3v_nrv(NS, TS);
@@ -982,8 +988,9 @@ __global__ void __launch_bounds__(t3v_max_threads<T>(), 2)
   constexpr int XS = t3v_xs(NS), KXR = t3v_kxr(NS), SK = STAGE_STRIDE;
   constexpr int HDR = 4 * LPS; // header vector(s) of a point block
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int sub = blockIdx.x;
-  const int tr = blockIdx.y;
+  const int sub = (int)(blockIdx.x / (unsigned)ntrx);
+  const int tr = (int)(blockIdx.y * (unsigned)ntrx + blockIdx.x % (unsigned)ntrx);
+  if (tr >= ntr) return;
   int b = L0.sub_bin[sub];
   PointLayout<T> Lg;
   const int64_t goff = resolve_problem<T>(L0, Lg, b);
@@ -2084,7 +2091,11 @@ template <typename T, int DIM> struct Dispatch {
           if (cfg.fixed) kv = spread_tile3v_kernel<T, NS, true>;
         GBN_CUDA(cudaFuncSetAttribute(kv, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)cfg.smem));
-        kv<<<grid, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total);
+        // transforms interleaved fastest; gridDim.x stays within 2^31 - 1
+        const int ntrx = (int)std::max<int64_t>(
+            1, std::min<int64_t>(ntr, INT32_MAX / std::max(L.nsub, 1)));
+        const dim3 gv((unsigned)L.nsub * (unsigned)ntrx, (unsigned)((ntr + ntrx - 1) / ntrx));
+        kv<<<gv, cfg.threads, cfg.smem, s>>>(L, K, c, pre, conj_pre, fw, nf_total, ntrx, ntr);
         GBN_LAUNCH_CHECK();
         return;
       }
