@@ -23,7 +23,7 @@ struct Arena {
 // cudaMallocAsync / cudaFreeAsync.
 // Stream-ordered pool of the current device for setpts scratch (keys,
 // records, sort buffers). It keeps freed memory for the next setpts instead of
-// returning it to the driver at every synchronisation (the default pool's
+// returning it to the CUDA driver at every synchronisation (the default pool's
 // behaviour), which would re-map gigabytes per call; gbnufft_trim_scratch
 // releases it.
 cudaMemPool_t scratch_pool();

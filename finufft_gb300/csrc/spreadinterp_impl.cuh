@@ -2018,7 +2018,7 @@ __global__ void __launch_bounds__(256)
 // ------------------------------------------------------------- dispatch ----
 // Tensor map of the fine grids for the TMA interpolation: rank dim + 1
 // (x, y, [z], transform), 8-byte elements (x counted in doubles for double
-// precision), box (BX, BY, BZ, 1). False when the driver rejects it.
+// precision), box (BX, BY, BZ, 1). False when the CUDA driver rejects it.
 template <typename T>
 bool encode_grid_map(CUtensorMap *map, const void *base, int dim, const int nf[3], int ntr,
                      int BX, int BY, int BZ) {

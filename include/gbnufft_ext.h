@@ -228,8 +228,8 @@ GBNUFFT_EXPORT int cufinufftf_spread_noalloc(int dim, const int64_t *n_grid, int
 
 /* setpts takes its temporary buffers (sort keys, coordinate records, radix  */
 /* sort storage) from a stream-ordered pool per device that keeps freed      */
-/* memory for the next setpts. This returns that memory to the driver for    */
-/* `device` (plans stay valid). 0 or a FINUFFT_ERR_* code.                    */
+/* memory for the next setpts. This returns that memory to the CUDA driver  */
+/* for `device` (plans stay valid). 0 or a FINUFFT_ERR_* code.                */
 GBNUFFT_EXPORT int gbnufft_trim_scratch(int device);
 
 /* Library build identification string. */
