@@ -2005,14 +2005,17 @@ __global__ void __launch_bounds__(INTERP_TILE_THREADS)
 
 // out[t*M + perm[p]] = src[t*M + p]: sorted-order interpolation results to user
 // order, transform by transform (blockIdx.y), so that the 8-byte scattered
-// writes of one transform combine into full sectors in L2
+// writes of one transform combine into full sectors in L2. The sorted results
+// and the permutation are read once per transform with evict-first
+// (cache-streaming) loads, so that they do not push the partly written output
+// lines out of L2 (16 vectors of 1e7 points: 5.69 -> 5.43 ms per execute).
 template <typename T>
 __global__ void __launch_bounds__(256)
     scatter_sorted_kernel(const cplx<T> *__restrict__ src, const int *__restrict__ perm, int M,
                           cplx<T> *__restrict__ out) {
   const int64_t o = (int64_t)blockIdx.y * M;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < M; p += gridDim.x * blockDim.x)
-    out[o + perm[p]] = src[o + p];
+    out[o + __ldcs(&perm[p])] = __ldcs(&src[o + p]);
 }
 
 // ------------------------------------------------------------- dispatch ----
