@@ -97,9 +97,11 @@ template <typename T> struct PointLayout {
   // 1 when points inside a bin are also sorted by cell (x fastest, z slowest)
   int cell_sorted = 0;
   // interpolation: when set (cplx<T>[ntr * M]), the tiled interpolation writes
-  // its results in sorted order here and a scatter pass per transform moves
-  // them to user order, so the scattered writes of one transform merge in L2
+  // its results in sorted order here and a gather pass per transform moves
+  // them to user order through iperm (the inverse of perm): coalesced writes,
+  // and the random reads of one transform's results hit L2
   void *sorted_out = nullptr;
+  const int *iperm = nullptr;
   // interpolation schedule: 0 auto, 1 gather per point, 2 shared-memory tiles
   int interp_mode = 0;
 };

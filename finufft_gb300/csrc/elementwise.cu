@@ -107,6 +107,8 @@ void launch_interp(const PointLayout<T> &L, const KernelShape<T> &K, const cplx<
                    int64_t nf_total, const cplx<T> *post, int conj_post, cplx<T> *out, int ntr,
                    cudaStream_t s) {
   if (L.nsub <= 0 || ntr <= 0) return;
+  // sorted-order results reach user order only through the inverse permutation
+  if (L.sorted_out && !L.iperm) GBN_THROW(FINUFFT_ERR_UNKNOWN_EXCEPTION, "sorted output without iperm");
   if (L.dim == 1) interp_dim<T, 1>(L, K, fw, nf_total, post, conj_post, out, ntr, s);
   else if (L.dim == 2) interp_dim<T, 2>(L, K, fw, nf_total, post, conj_post, out, ntr, s);
   else interp_dim<T, 3>(L, K, fw, nf_total, post, conj_post, out, ntr, s);
@@ -499,5 +501,18 @@ double smem_atomic_rate(int device, bool i32) {
                                         const QuadNodes &, cplx<T> *, cudaStream_t);
 GBN_INST(float)
 GBN_INST(double)
+
+// iperm[perm[p]] = p: the inverse of the sort permutation, for the type-2
+// gather from sorted-order results to user order
+__global__ void invert_perm_kernel(const int *__restrict__ perm, int M, int *__restrict__ iperm) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < M; p += gridDim.x * blockDim.x)
+    iperm[perm[p]] = p;
+}
+void launch_invert_perm(const int *perm, int M, int *iperm, cudaStream_t s) {
+  if (M <= 0) return;
+  const unsigned g = (unsigned)std::min<int64_t>((M + 255) / 256, 152 * 8);
+  invert_perm_kernel<<<g, 256, 0, s>>>(perm, M, iperm);
+  GBN_LAUNCH_CHECK();
+}
 
 } // namespace gbn

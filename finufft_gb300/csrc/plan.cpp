@@ -631,6 +631,7 @@ template <typename T> PointLayout<T> Plan<T>::layout() const {
   L.perm = perm.p;
   L.cell_sorted = cell_sorted;
   L.sorted_out = isort.p;
+  L.iperm = isort.p ? iperm.p : nullptr;
   // method 1 (asked for, or the reference heuristic's choice for type 2)
   // interpolates one point per thread from the grid, as the reference's
   // method 1 does; method 2 uses the tiled schedules
@@ -691,25 +692,32 @@ void Plan<T>::sort_points(int64_t Mp, const T *const xyz[3], const AxisMap ax[3]
   sub_count_.p = sa.count;
   sub_bin_.n = sub_start_.n = sub_count_.n = sa.cap;
   // 2D type-2 batches whose per-transform output fits in L2: interpolate into
-  // sorted order, then scatter transform by transform (16 vectors of 1e7 2D
-  // points, batches of 16: 5.72 ms against 6.84 ms writing user order from the
-  // interpolation). Not in 3D, where the interpolation's own scattered writes
-  // cost less than the extra pass (1.25e7 clustered points, 4 vectors at 128^3:
-  // 4.98 ms direct, 5.85 ms through the sorted copy). The sorted copy of a
-  // batch's outputs is only taken when it costs at most an eighth of the
-  // device memory free at setpts. gbnufft_opts.interp_mode 1 or 2 writes user
-  // order directly.
+  // sorted order, then gather transform by transform into user order through
+  // the inverse permutation (coalesced writes; the random reads of one
+  // transform's sorted results hit L2). 16 vectors of 1e7 2D points, batches
+  // of 16: 3.70 ms per execute, against 5.09 ms scattering through perm and
+  // 6.84 ms writing user order from the interpolation. Not in 3D, where the
+  // interpolation's own scattered writes cost less than the extra pass in
+  // the scatter form (1.25e7 clustered points, 4 vectors at 128^3: 4.98 ms
+  // direct, 5.85 ms through the sorted copy). The sorted copy of a batch's
+  // outputs is only taken when it costs at most an eighth of the device
+  // memory free at setpts. gbnufft_opts.interp_mode 1 or 2 writes user order
+  // directly.
   isort.release();
+  iperm.release();
   if (type == 2 && batchsize > 1 && batchsize <= 65535 && dim == 2 && M > 0 &&
-      ext.interp_mode == 0 && method != 1) { // (the scatter's grid has one row per transform)
+      ext.interp_mode == 0 && method != 1) { // (the gather's grid has one row per transform)
     int dev = 0, l2 = 0;
     GBN_CUDA(cudaGetDevice(&dev));
     GBN_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
     size_t freeb = 0, totb = 0;
     GBN_CUDA(cudaMemGetInfo(&freeb, &totb));
-    const double bytes = (double)batchsize * M * sizeof(cplx<T>);
-    if ((double)M * sizeof(cplx<T>) <= 0.75 * (double)l2 && bytes <= 0.125 * (double)freeb)
+    const double bytes = (double)batchsize * M * sizeof(cplx<T>) + (double)M * sizeof(int);
+    if ((double)M * sizeof(cplx<T>) <= 0.75 * (double)l2 && bytes <= 0.125 * (double)freeb) {
       isort.resize((size_t)batchsize * M);
+      iperm.resize((size_t)M);
+      launch_invert_perm(perm.p, (int)M, iperm.p, stream);
+    }
   }
 }
 

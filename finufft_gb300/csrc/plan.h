@@ -161,6 +161,7 @@ private:
   DevArray<cplx<T>> t3pre;     // type 3 pre-phase, M
   DevArray<cplx<T>> t3post;    // type 3 post factor, N
   DevArray<cplx<T>> isort;     // type 2: sorted-order interpolation output, batchsize * M
+  DevArray<int> iperm;         // with isort: iperm[perm[p]] = p, M
   bool pts_set = false;
   SpreadConfig scfg{2, 256, 0};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};

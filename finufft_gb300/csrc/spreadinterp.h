@@ -32,6 +32,9 @@ size_t spread_tile3x_bytes(int ns, const int bin[3]);
 int *device_error_word();
 int device_error_take();
 
+// iperm[perm[p]] = p for p < M (perm a permutation of 0 .. M-1).
+void launch_invert_perm(const int *perm, int M, int *iperm, cudaStream_t s);
+
 // fw[t*nf + g] += sum_j c[t*M + j] (* pre[j] or conj(pre[j])) phi(g - x_j), t < ntr.
 // fw must be zeroed by the caller.
 template <typename T>

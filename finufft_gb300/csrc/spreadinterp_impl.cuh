@@ -2003,19 +2003,20 @@ __global__ void __launch_bounds__(INTERP_TILE_THREADS)
 
 #include "interp_tma.cuh"
 
-// out[t*M + perm[p]] = src[t*M + p]: sorted-order interpolation results to user
-// order, transform by transform (blockIdx.y), so that the 8-byte scattered
-// writes of one transform combine into full sectors in L2. The sorted results
-// and the permutation are read once per transform with evict-first
-// (cache-streaming) loads, so that they do not push the partly written output
-// lines out of L2 (16 vectors of 1e7 points: 5.69 -> 5.43 ms per execute).
+// out[t*M + j] = src[t*M + iperm[j]]: sorted-order interpolation results to
+// user order, transform by transform (blockIdx.y). The writes are coalesced
+// and evict-first, as are the loads of the inverse permutation; the random
+// 8-byte reads fall in one transform's sorted results, which stay in L2. (16
+// vectors of 1e7 2D points: 3.70 ms per execute, against 5.09 ms for the
+// scatter out[t*M + perm[p]] = src[t*M + p], whose partial-sector writes had to
+// merge in L2.)
 template <typename T>
 __global__ void __launch_bounds__(256)
-    scatter_sorted_kernel(const cplx<T> *__restrict__ src, const int *__restrict__ perm, int M,
-                          cplx<T> *__restrict__ out) {
+    gather_sorted_kernel(const cplx<T> *__restrict__ src, const int *__restrict__ iperm, int M,
+                         cplx<T> *__restrict__ out) {
   const int64_t o = (int64_t)blockIdx.y * M;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < M; p += gridDim.x * blockDim.x)
-    out[o + __ldcs(&perm[p])] = __ldcs(&src[o + p]);
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x)
+    __stcs(&out[o + j], src[o + __ldcs(&iperm[j])]);
 }
 
 // ------------------------------------------------------------- dispatch ----
@@ -2178,8 +2179,8 @@ template <typename T, int DIM> struct Dispatch {
           GBN_LAUNCH_CHECK();
           if (L.sorted_out) {
             const unsigned gx = (unsigned)std::min<int64_t>((L.M + 255) / 256, 152 * 8);
-            scatter_sorted_kernel<T><<<dim3(gx, (unsigned)ntr), 256, 0, s>>>(
-                static_cast<const cplx<T> *>(L.sorted_out), L.perm, L.M, out);
+            gather_sorted_kernel<T><<<dim3(gx, (unsigned)ntr), 256, 0, s>>>(
+                static_cast<const cplx<T> *>(L.sorted_out), L.iperm, L.M, out);
             GBN_LAUNCH_CHECK();
           }
           return;
@@ -2208,8 +2209,8 @@ template <typename T, int DIM> struct Dispatch {
         GBN_LAUNCH_CHECK();
         if (L.sorted_out && L.M > 0) {
           const unsigned gx = (unsigned)std::min<int64_t>((L.M + 255) / 256, 152 * 8);
-          scatter_sorted_kernel<T><<<dim3(gx, (unsigned)ntr), 256, 0, s>>>(
-              static_cast<const cplx<T> *>(L.sorted_out), L.perm, L.M, out);
+          gather_sorted_kernel<T><<<dim3(gx, (unsigned)ntr), 256, 0, s>>>(
+              static_cast<const cplx<T> *>(L.sorted_out), L.iperm, L.M, out);
           GBN_LAUNCH_CHECK();
         }
         return;
